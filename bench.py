@@ -1,0 +1,323 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 pairwise-alignment path.
+
+Workload (one "step"): 100,000 protein pairs of uneven length (log-normal,
+median 350, sigma 0.5, clipped 50..2,000; partner at 30..90 % identity with
+5 % indels; seed 2), BLOSUM62, gap open 11 / extend 1, global, score only --
+about 2.0e10 DP cells.  Metric: GCUPS (giga cell updates per second).
+
+  value  batched form: the planned, length-bucketed persistent launches of a
+         device-resident batch replayed as a CUDA graph, inputs already in
+         HBM; CUDA events on the batch's own stream around each step; L2
+         flushed (256 MB memset on that stream) between timed steps.
+  e2e    the same metric through the C ABI entry point tsq_align_batch with
+         host buffers: pinned host residues and pair table copied in, results
+         copied back, every step.
+  plain  one tsq_align_pair call (one launch sequence) per pair over a
+         sample of the same pairs: the per-pair GPU path batching is
+         measured against.
+
+``--impl reference`` times the CPU implementation of the path (the oracle,
+all host cores) on a bounded sample of the same workload.
+
+Multi-GPU: pairs are independent, so N GPUs run N replicas of the workload
+(weak scaling) with no data-path collective; rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = ("uneven_pairs_100k: 100,000 protein pairs, lengths log-normal (median 350, sigma 0.5, clipped 50-2000), "
+            "partner 30-90% identity with 5% indels, seed 2; BLOSUM62, gap 11/1, global, score only")
+METRIC = "GCUPS (batched, 100k uneven protein pairs, score-only, bit-exact)"
+CPU_SAMPLE_PAIRS = 20000
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--plain-pairs", type=int, default=2000)
+    ap.add_argument("--e2e-steps", type=int, default=0, help="0 = same as --steps")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sms, maxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                maxs.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sms:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sms)), "sm_max_mhz": float(max(maxs)), "reasons": sorted(reasons),
+                "samples": len(sms)}
+
+
+def traffic_from_profile():
+    """DRAM bytes per fill launch recorded from ncu in profiles/ (or None)."""
+    path = os.path.join(ROOT, "profiles", "fill_uneven_pairs_100k.md")
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", text)
+    return float(m.group(1)) if m else None
+
+
+def cpu_leg(ps, sample_pairs, steps=1, warmup=0):
+    """The oracle (CPU restatement of the path) on all host cores over a
+    bounded, seeded sample of the workload."""
+    from oracle import oracle as O
+    O.build()
+    rng = np.random.default_rng(12345)
+    idx = np.sort(rng.choice(len(ps), size=min(sample_pairs, len(ps)), replace=False))
+    sub = ps.subset(idx)
+    cores = O.num_cores()
+    times, out = [], None
+    for k in range(warmup + steps):
+        t0 = time.perf_counter()
+        out = O.batch(sub.seqs, sub.a_off, sub.a_len, sub.b_off, sub.b_len, ps.matrix, ps.gap_open, ps.gap_extend,
+                      False, O.MODE_SCORE, cores)
+        dt = time.perf_counter() - t0
+        if k >= warmup:
+            times.append(dt)
+    gcups = sub.cells / float(np.mean(times)) / 1e9
+    return {"value": gcups, "unit": "GCUPS", "cores": cores, "kind": "port",
+            "sample": f"{len(idx)} of the 100,000 pairs (seeded subset, {sub.cells:.3e} cells), all host cores",
+            "seconds_per_sample": float(np.mean(times))}, idx, out
+
+
+def run_reference(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    from tweakseq_gb300 import workloads as W
+    ps = W.uneven_pairs()
+    base, _, _ = cpu_leg(ps, CPU_SAMPLE_PAIRS, steps=args.steps, warmup=args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": base["value"], "unit": "GCUPS", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["seconds_per_sample"] * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded generator; no public dataset is named for this path)",
+        "config": {"workload": WORKLOAD, "sample_pairs": CPU_SAMPLE_PAIRS},
+        "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": base["value"], "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference (groundstate/tweakseq) has no in-tree pairwise DP; its CPU path for this arm is "
+                "the project's CPU restatement (oracle/), run on every host core",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from tweakseq_gb300 import aligner as A
+    from tweakseq_gb300 import build as B
+    from tweakseq_gb300 import workloads as W
+
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    B.build()
+    ps = W.uneven_pairs()
+    cells = ps.cells
+
+    # ---- value: device-resident batch, graph replay --------------------------
+    batch = A.Batch(ps, output="score", use_graph=True)
+    ext = torch.cuda.ExternalStream(batch.stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        batch.run()
+    st = batch.stats()
+    launches_per_step = int(st["launches"])
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    step_ms, fill_ms = [], []
+    barrier()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(ext):
+                flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            batch.run_async()
+            e1.record(ext)
+            batch.sync()
+            step_ms.append(e0.elapsed_time(e1))
+            fill_ms.append(batch.stats()["fill_ms"])
+        barrier()
+    total_ms = float(np.sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * cells * args.steps / (total_ms * 1e-3) / 1e9
+    res_dev = batch.results()
+
+    # ---- e2e: C ABI with host buffers --------------------------------------
+    e2e_steps = args.e2e_steps or args.steps
+    pinned = torch.empty(len(ps.seqs), dtype=torch.uint8, pin_memory=True)
+    pinned.numpy()[:] = ps.seqs
+    host_ps = W.PairSet(pinned.numpy(), ps.a_off, ps.a_len, ps.b_off, ps.b_len)
+    A.align_batch(host_ps, output="score")  # warm the cached engine
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        res_e2e = A.align_batch(host_ps, output="score")
+    e2e_s = time.perf_counter() - t0
+    barrier()
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * cells * e2e_steps / e2e_s / 1e9
+    h2d = int(len(ps.seqs) + 24 * len(ps))
+    d2h = int(32 * len(ps))
+    assert np.array_equal(res_e2e.table["score"], res_dev.table["score"])
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    # ---- plain per-pair path over a sample ------------------------------------
+    P = min(args.plain_pairs, len(ps))
+    plain_cells = int(np.dot(ps.a_len[:P].astype(np.int64), ps.b_len[:P].astype(np.int64)))
+    a0, b0 = ps.pair(0)
+    A.align_pair(a0, b0, output="score")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain_scores = np.empty(P, dtype=np.int64)
+    for k in range(P):
+        a, b = ps.pair(k)
+        plain_scores[k] = A.align_pair(a, b, output="score").score
+    plain_s = time.perf_counter() - t0
+    plain_gcups = plain_cells / plain_s / 1e9
+    assert np.array_equal(plain_scores, res_dev.table["score"][:P])
+
+    # ---- roofline of the fill ---------------------------------------------
+    dpx_rate = A.probe_dpx(packed=False)  # int32 DPX-class instructions / lane / s
+    peak_gcups = dpx_rate / 4.0 / 1e9      # 4 DPX-class instructions per cell
+    fill_avg_ms = float(np.mean(fill_ms))
+    achieved = cells / (fill_avg_ms * 1e-3) / 1e9
+    roofline = {"bound": "int", "achieved": achieved, "peak": peak_gcups, "unit": "Gcell/s",
+                "frac": achieved / peak_gcups, "traffic": traffic_from_profile(),
+                "peak_source": "measured live: tsq_probe_dpx int32 DPX rate / 4 instructions per cell",
+                "kernel": "fill_i32_kernel (score, global)", "fill_ms_avg": fill_avg_ms}
+
+    # ---- CPU baseline (the oracle on this host) ----------------------------
+    cpu = None
+    bitexact = None
+    if not args.no_cpu:
+        cpu, idx, want = cpu_leg(ps, CPU_SAMPLE_PAIRS)
+        mism = int(np.count_nonzero(res_dev.table["score"][idx] != want["score"]))
+        bitexact = {"pairs_checked": int(len(idx)), "mismatches": mism}
+        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded generator with the workload's shapes and distributions; no public dataset)",
+        "config": {"workload": WORKLOAD, "pairs": len(ps), "cells": cells, "parallelism": f"replicas x{world}",
+                   "l2": "flushed between timed steps (256 MB memset on the launch stream)",
+                   "launch": "device-resident batch, CUDA graph replay"},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "GCUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "steps": e2e_steps, "api": "tsq_align_batch (pinned host residues in, host results out)"},
+        "plain": {"gcups": plain_gcups, "pairs": P, "ms_per_pair": plain_s / P * 1e3,
+                  "api": "tsq_align_pair, one launch sequence per pair"},
+        "batched_over_plain": value / plain_gcups,
+        "bitexact": bitexact,
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

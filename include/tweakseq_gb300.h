@@ -1,0 +1,187 @@
+/*
+ * tweakseq_gb300.h -- C ABI of the GB300 pairwise-alignment library.
+ *
+ * The reference, groundstate/tweakseq, has no in-process pairwise alignment
+ * call.  Its only seam for alignment is the AlignmentTool plugin
+ * (tweakseq/Core/AlignmentTool.h:36-71): Project exports the selected
+ * sequences as FASTA (tweakseq/Core/Project.cpp:870-894),
+ * SeqEditMainWin::startAlignment runs the tool's command line through
+ * QProcess (tweakseq/UI/SeqEditMainWin.cpp:1616-1663), and
+ * Project::readNewAlignment reads back one gapped string per label
+ * (tweakseq/Core/Project.cpp:908-1032).  The entry points below replace the
+ * external process behind that seam: they take the residues the editor
+ * would have written (Sequence::filter output, tweakseq/Core/Sequence.cpp:57-69:
+ * uppercase ASCII, flag bits already stripped) and return the equal-length
+ * gapped strings, with '-' as the gap character as the editor uses it
+ * (tweakseq/Core/Sequences.cpp:266-287), that readNewAlignment consumes.
+ *
+ * Scoring: BLOSUM62 with the reference's letter map
+ * (tweakseq/Core/Annotations/Consensus.cpp:34-69; J, O, U score as X), DNA
+ * (+2 / -3 over IUPAC letters) or a caller-supplied 26x26 int8 matrix.  A gap
+ * of length k costs gap_open + k * gap_extend.  Tie-breaks, identity and
+ * coordinates follow the conventions stated in the library's documentation
+ * and are bit-exact against the project's CPU oracle.
+ *
+ * Every function returns an int status: TSQ_OK (0) or a negative TSQ_E_*
+ * code.  Nothing throws across the ABI.  There is no CPU fallback: without a
+ * usable CUDA device the calls return TSQ_E_CUDA.
+ */
+#ifndef TWEAKSEQ_GB300_H_
+#define TWEAKSEQ_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TSQ_ABI_VERSION 1
+
+/* Status codes. */
+#define TSQ_OK 0
+#define TSQ_E_INVALID_ARG (-1)
+#define TSQ_E_INVALID_RESIDUE (-2) /* byte outside 'A'..'Z' or not valid for the matrix */
+#define TSQ_E_NOMEM (-3)           /* host or device allocation failed */
+#define TSQ_E_CUDA (-4)            /* CUDA error or no device */
+#define TSQ_E_TIMEOUT (-5)         /* a bounded device-side wait ran out */
+#define TSQ_E_PENDING (-6)         /* server request not finished yet */
+#define TSQ_E_REJECTED (-7)        /* request can never fit the server's HBM budget */
+#define TSQ_E_NOT_FOUND (-8)       /* unknown server request id */
+#define TSQ_E_CANCELLED (-9)       /* request cancelled before it ran */
+#define TSQ_E_TOO_LARGE (-10)      /* input beyond a fixed capacity */
+
+/* Scoring matrices. */
+#define TSQ_MATRIX_BLOSUM62 0
+#define TSQ_MATRIX_DNA 1
+#define TSQ_MATRIX_CUSTOM 2
+
+/* Alignment modes. */
+#define TSQ_GLOBAL 0
+#define TSQ_LOCAL 1
+
+/* What to compute. */
+#define TSQ_OUT_SCORE 0     /* score (local: plus end coordinates) */
+#define TSQ_OUT_IDENTITY 1  /* score, n_ident and n_cols, no strings */
+#define TSQ_OUT_ALIGNMENT 2 /* everything, gapped strings included */
+
+/* DP lane width. */
+#define TSQ_LANE_AUTO 0 /* int16x2 where it is exact, int32 otherwise */
+#define TSQ_LANE_I16 1  /* int16x2 with overflow detection, int32 re-run on overflow */
+#define TSQ_LANE_I32 2  /* int32 only */
+
+typedef struct {
+  int32_t matrix;              /* TSQ_MATRIX_* */
+  int32_t gap_open;            /* >= 0 */
+  int32_t gap_extend;          /* >= 0 */
+  int32_t mode;                /* TSQ_GLOBAL or TSQ_LOCAL */
+  int32_t output;              /* TSQ_OUT_* */
+  int32_t lane;                /* TSQ_LANE_* */
+  const int8_t *custom_score;  /* 26*26, [x][y] for 'A'+x vs 'A'+y (TSQ_MATRIX_CUSTOM) */
+  const uint8_t *custom_valid; /* 26 flags (TSQ_MATRIX_CUSTOM) */
+} tsq_params;
+
+/* Result of one pair.  Coordinates are 0-based half-open: a[a_begin:a_end]
+ * is aligned against b[b_begin:b_end].  Fields a mode does not compute are
+ * -1 (begins for TSQ_OUT_SCORE local; n_ident/n_cols for TSQ_OUT_SCORE).
+ * aln_a / aln_b are NUL-terminated, allocated by the library for
+ * TSQ_OUT_ALIGNMENT and released by tsq_result_free; otherwise NULL. */
+typedef struct {
+  int32_t score;
+  int32_t a_begin, a_end, b_begin, b_end;
+  int32_t n_ident, n_cols;
+  int32_t status; /* per-pair status (TSQ_OK or TSQ_E_INVALID_RESIDUE) */
+  char *aln_a;
+  char *aln_b;
+} tsq_result;
+
+/* One pair of a batch: offsets and lengths into the batch's residue buffer. */
+typedef struct {
+  int64_t a_off, b_off;
+  int32_t a_len, b_len;
+} tsq_pair_desc;
+
+typedef struct {
+  int32_t device;       /* CUDA ordinal; -1 = current device */
+  int32_t use_graph;    /* 1 = replay the launch sequence as a CUDA graph */
+  int32_t autotune;     /* 1 = consult the tuned table (tsq_tune_load) */
+  int32_t reserved;
+} tsq_batch_opts;
+
+/* Counters of the last run of a batch. */
+typedef struct {
+  int64_t cells;           /* sum of m*n over the pairs */
+  int64_t pairs;
+  int64_t rerun_pairs;     /* pairs re-run in int32 after int16 overflow */
+  int32_t launches;        /* kernel launches per run */
+  int32_t buckets;         /* length buckets used */
+  double device_ms;        /* device time of the last run (CUDA events) */
+  double fill_ms;          /* of which the fill kernels */
+} tsq_batch_stats;
+
+/* ---- Version / device ---------------------------------------------------- */
+
+/* ABI version and a static build description string. */
+int tsq_version(int32_t *abi_version, const char **build);
+
+/* ---- Plain form: one pair per call -------------------------------------- */
+
+/* Aligns a (length la) with b (length lb) on the current CUDA device: one
+ * launch sequence for this pair alone.  Fills *out; free it with
+ * tsq_result_free. */
+int tsq_align_pair(const uint8_t *a, int32_t la, const uint8_t *b, int32_t lb,
+                   const tsq_params *p, tsq_result *out);
+
+/* Releases the strings of one result (safe on results without strings). */
+void tsq_result_free(tsq_result *r);
+/* Releases the strings of n results. */
+void tsq_results_free(tsq_result *r, int64_t n);
+
+/* ---- Batched form -------------------------------------------------------- */
+
+/* Aligns n pairs over one host residue buffer in one planned launch
+ * sequence (length buckets, persistent kernels, optional CUDA graph).
+ * out[k] receives pair k.  Returns TSQ_E_INVALID_RESIDUE if any pair holds
+ * an invalid residue (that pair's status says so; the others are valid). */
+int tsq_align_batch(const uint8_t *seqs, int64_t seqs_len,
+                    const tsq_pair_desc *pairs, int64_t n, const tsq_params *p,
+                    const tsq_batch_opts *opts, tsq_result *out);
+
+/* Device-resident batch: upload and plan once, run many times, read back. */
+typedef struct tsq_batch tsq_batch;
+int tsq_batch_create(const uint8_t *seqs, int64_t seqs_len,
+                     const tsq_pair_desc *pairs, int64_t n, const tsq_params *p,
+                     const tsq_batch_opts *opts, tsq_batch **out);
+/* Enqueues one run on the batch's stream and waits for it. */
+int tsq_batch_run(tsq_batch *b);
+/* Enqueues one run without waiting (tsq_batch_sync waits). */
+int tsq_batch_run_async(tsq_batch *b);
+int tsq_batch_sync(tsq_batch *b);
+/* Copies results of the last run to the host (strings allocated as above). */
+int tsq_batch_results(tsq_batch *b, tsq_result *out);
+int tsq_batch_get_stats(const tsq_batch *b, tsq_batch_stats *st);
+/* The CUDA stream (cudaStream_t) the batch runs on, for event timing. */
+int tsq_batch_stream(const tsq_batch *b, void **stream);
+void tsq_batch_destroy(tsq_batch *b);
+
+/* ---- Autotuner ------------------------------------------------------------ */
+
+/* Measures the compiled kernel shapes on the current device over seeded
+ * synthetic pairs and writes the per-length-bucket choice as JSON. */
+int tsq_tune_run(const char *json_path, int32_t quick);
+/* Loads a tuned table written by tsq_tune_run (used when opts->autotune). */
+int tsq_tune_load(const char *json_path);
+
+/* ---- Device probe ---------------------------------------------------------- */
+
+/* Measured rate of the DP fill's DPX-class instructions (add-then-max and
+ * three-way max) on the current device, in instructions per lane per second;
+ * packed = 0 for the int32 forms, 1 for the int16x2 forms (two cells per
+ * instruction).  This is the denominator of the fill's roofline. */
+int tsq_probe_dpx(int32_t packed, double *instr_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TWEAKSEQ_GB300_H_ */

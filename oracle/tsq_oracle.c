@@ -322,7 +322,7 @@ int tsqo_score(const uint8_t *a, int32_t m, const uint8_t *b, int32_t n,
     out->score = best;
     out->a_end = bi;
     out->b_end = bj;
-    out->a_begin = out->b_begin = -1;
+    out->a_begin = out->b_begin = best > 0 ? -1 : 0;
   } else {
     out->score = H[n];
     out->a_begin = 0;

@@ -87,7 +87,8 @@ int tsqo_align(const uint8_t *a, int32_t m, const uint8_t *b, int32_t n,
 
 /* Linear-space score-only fill.  Global: score only (coordinates set to the
  * full span, counts to -1).  Local: score and end coordinates a_end/b_end of
- * the first maximal cell (begins and counts set to -1). */
+ * the first maximal cell (begins -1, or 0 when the alignment is empty;
+ * counts -1). */
 int tsqo_score(const uint8_t *a, int32_t m, const uint8_t *b, int32_t n,
                const tsqo_scheme *sc, int32_t gap_open, int32_t gap_extend,
                int32_t local, tsqo_result *out);

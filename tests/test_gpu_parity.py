@@ -1,0 +1,229 @@
+"""GPU parity: the CUDA library, called through its C ABI, against the CPU
+oracle on the same seeded inputs.  Integer work, so the bar is bit-exact:
+scores, coordinates, identity counts and both gapped strings."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tweakseq_gb300 import _native as N
+from tweakseq_gb300 import aligner as A
+from tweakseq_gb300 import build as B
+from tweakseq_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+FIELDS = ("score", "a_begin", "a_end", "b_begin", "b_end", "n_ident", "n_cols")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    B.build()
+    O.build()
+    N.lib()
+
+
+def oracle_batch(ps, local, mode, strings=False, nthreads=0):
+    return O.batch(ps.seqs, ps.a_off, ps.a_len, ps.b_off, ps.b_len, ps.matrix, ps.gap_open, ps.gap_extend, local,
+                   mode, nthreads, strings)
+
+
+def gpu_batch(ps, local, output, **kw):
+    return A.align_batch(ps, matrix=ps.matrix, gap_open=ps.gap_open, gap_extend=ps.gap_extend,
+                         mode="local" if local else "global", output=output, **kw)
+
+
+def assert_same(got, want, fields, what):
+    for f in fields:
+        bad = np.flatnonzero(got.table[f] != want[f])
+        assert len(bad) == 0, f"{what}: field {f} differs at pairs {bad[:10].tolist()} " \
+                              f"(gpu {got.table[f][bad[:3]].tolist()} vs oracle {want[f][bad[:3]].tolist()})"
+
+
+def score_fields(local):
+    return ("score", "a_end", "b_end") if local else ("score",)
+
+
+def ident_fields(local):
+    return ("score", "a_end", "b_end", "n_ident", "n_cols") if local else ("score", "n_ident", "n_cols")
+
+
+def test_golden_cases_plain_path():
+    cases = json.load(open(os.path.join(GOLDEN, "oracle_cases.json")))
+    for c in cases:
+        r = A.align_pair(c["a"], c["b"], matrix=c["matrix"], gap_open=c["gap_open"], gap_extend=c["gap_extend"],
+                         mode="local" if c["local"] else "global", output="alignment")
+        got = (r.score, r.a_begin, r.a_end, r.b_begin, r.b_end, r.n_ident, r.n_cols, r.aln_a, r.aln_b)
+        want = tuple(c[k] for k in FIELDS + ("aln_a", "aln_b"))
+        assert got == want, c["name"]
+        s = A.align_pair(c["a"], c["b"], matrix=c["matrix"], gap_open=c["gap_open"], gap_extend=c["gap_extend"],
+                         mode="local" if c["local"] else "global", output="score")
+        assert s.score == c["score"], c["name"]
+        i = A.align_pair(c["a"], c["b"], matrix=c["matrix"], gap_open=c["gap_open"], gap_extend=c["gap_extend"],
+                         mode="local" if c["local"] else "global", output="identity")
+        assert (i.score, i.n_ident, i.n_cols) == (c["score"], c["n_ident"], c["n_cols"]), c["name"]
+
+
+def random_pairs(seed, n, lo, hi, dna=False, related=0.5):
+    rng = np.random.default_rng(seed)
+    seqs, pairs = [], []
+    for k in range(n):
+        m = int(rng.integers(lo, hi + 1))
+        if dna:
+            a = W.DNA_LETTERS[rng.integers(0, 4, m)]
+        else:
+            a = W.random_protein(rng, m)
+        if rng.random() < related and m > 0:
+            if dna:
+                b = W._mutate_dna(rng, a, 0.1, 0.02, 3.0)
+            else:
+                b, _ = W._mutate_proteins(rng, a, np.array([m]), np.array([0.5]), 0.05)
+        else:
+            nn = int(rng.integers(lo, hi + 1))
+            b = W.DNA_LETTERS[rng.integers(0, 4, nn)] if dna else W.random_protein(rng, nn)
+        seqs += [a.tobytes(), b.tobytes()]
+        pairs.append((2 * k, 2 * k + 1))
+    kw = dict(matrix=W.DNA, gap_open=5, gap_extend=2) if dna else {}
+    return W._pairset_from_lists(seqs, pairs, **kw)
+
+
+@pytest.mark.parametrize("local", [False, True])
+@pytest.mark.parametrize("output", ["score", "identity", "alignment"])
+def test_random_uneven_protein(local, output):
+    ps = random_pairs(100 + local, 600, 0, 700)
+    got = gpu_batch(ps, local, output)
+    if output == "alignment":
+        want, sa, sb = oracle_batch(ps, local, O.MODE_ALIGN, strings=True)
+        assert_same(got, want, FIELDS, "alignment")
+        assert got.aln_a == sa and got.aln_b == sb
+    elif output == "identity":
+        want = oracle_batch(ps, local, O.MODE_IDENT)
+        assert_same(got, want, ident_fields(local), "identity")
+    else:
+        want = oracle_batch(ps, local, O.MODE_SCORE)
+        assert_same(got, want, score_fields(local), "score")
+
+
+@pytest.mark.parametrize("local", [False, True])
+def test_low_complexity_ties(local):
+    """Homopolymers and short repeats create many equal-score paths: the
+    tie-breaks decide every traceback."""
+    seqs, pairs = [], []
+    motifs = [b"A", b"AG", b"GGA", b"W", b"KR", b"ACGT"]
+    rng = np.random.default_rng(9)
+    for k in range(120):
+        ma, mb = motifs[k % len(motifs)], motifs[(k // 3) % len(motifs)]
+        a = (ma * 400)[: int(rng.integers(1, 300))]
+        b = (mb * 400)[: int(rng.integers(1, 300))]
+        seqs += [a, b]
+        pairs.append((2 * k, 2 * k + 1))
+    for gaps in ((11, 1), (0, 1), (3, 0)):
+        ps = W._pairset_from_lists(seqs, pairs, gap_open=gaps[0], gap_extend=gaps[1])
+        got = gpu_batch(ps, local, "alignment")
+        want, sa, sb = oracle_batch(ps, local, O.MODE_ALIGN, strings=True)
+        assert_same(got, want, FIELDS, f"ties {gaps}")
+        assert got.aln_a == sa and got.aln_b == sb
+
+
+def test_all_vs_all_64_proteins_alignment():
+    """64 proteins (lengths 200-400, seed 1), all 2,016 global pairs with
+    full traceback: scores, strings and identity bit-exact."""
+    ps = W.all_vs_all_proteins()
+    got = gpu_batch(ps, False, "alignment")
+    want, sa, sb = oracle_batch(ps, False, O.MODE_ALIGN, strings=True)
+    assert_same(got, want, FIELDS, "c1")
+    assert got.aln_a == sa and got.aln_b == sb
+
+
+def test_uneven_pairs_score_full():
+    """All 100,000 uneven pairs (log-normal lengths 50-2,000), score only."""
+    ps = W.uneven_pairs()
+    got = gpu_batch(ps, False, "score")
+    want = oracle_batch(ps, False, O.MODE_SCORE)
+    assert_same(got, want, ("score",), "c2")
+
+
+def test_dna_long_traceback():
+    ps = random_pairs(7, 6, 1500, 4000, dna=True, related=1.0)
+    for local in (False, True):
+        got = gpu_batch(ps, local, "alignment")
+        want, sa, sb = oracle_batch(ps, local, O.MODE_ALIGN, strings=True)
+        assert_same(got, want, FIELDS, "dna")
+        assert got.aln_a == sa and got.aln_b == sb
+
+
+def test_guide_tree_identity_sample():
+    ps = W.guide_tree_families(n_families=3, per_family=30)
+    got = gpu_batch(ps, False, "identity")
+    want = oracle_batch(ps, False, O.MODE_IDENT)
+    assert_same(got, want, ("score", "n_ident", "n_cols"), "c4 sample")
+
+
+def test_invalid_residues_reported_per_pair():
+    seqs = [b"ACDEFG", b"ACDXFG", b"acdefg", b"ACD", b"AC-DE", b"", b"A1"]
+    pairs = [(0, 1), (0, 2), (3, 0), (4, 3), (5, 6), (5, 0)]
+    ps = W._pairset_from_lists(seqs, pairs)
+    with pytest.raises(N.TsqError) as e:
+        gpu_batch(ps, False, "alignment")
+    assert e.value.rc == N.E_INVALID_RESIDUE
+    got = gpu_batch(ps, False, "alignment", check=False)
+    assert got.table["status"].tolist() == [0, -2, 0, -2, -2, 0]
+    ok = [0, 2, 5]
+    want, sa, sb = oracle_batch(ps.subset(ok), False, O.MODE_ALIGN, strings=True)
+    for j, k in enumerate(ok):
+        assert got.table["score"][k] == want["score"][j] and got.aln_a[k] == sa[j] and got.aln_b[k] == sb[j]
+    with pytest.raises(N.TsqError) as e:
+        A.align_pair(b"ACGE", b"ACGT", matrix="dna", gap_open=5, gap_extend=2)
+    assert e.value.rc == N.E_INVALID_RESIDUE
+
+
+def test_bad_arguments_rejected():
+    with pytest.raises(N.TsqError) as e:
+        A.align_pair(b"ACD", b"ACD", gap_open=-1)
+    assert e.value.rc == N.E_INVALID_ARG
+    ps = W._pairset_from_lists([b"ACD", b"ACD"], [(0, 1)])
+    ps.a_off = ps.a_off + 5  # out of the residue buffer
+    with pytest.raises(N.TsqError) as e:
+        gpu_batch(ps, False, "score")
+    assert e.value.rc == N.E_INVALID_ARG
+
+
+def test_custom_matrix_asymmetric():
+    rng = np.random.default_rng(3)
+    mat = rng.integers(-6, 9, size=(26, 26)).astype(np.int8)
+    valid = np.ones(26, np.uint8)
+    valid[ord("Z") - 65] = 0
+    ps = random_pairs(11, 80, 1, 200)
+    for local in (False, True):
+        got = A.align_batch(ps, custom=(mat, valid), gap_open=4, gap_extend=2,
+                            mode="local" if local else "global", output="alignment")
+        want, sa, sb = O.batch(ps.seqs, ps.a_off, ps.a_len, ps.b_off, ps.b_len, (mat, valid), 4, 2, local,
+                               O.MODE_ALIGN, 0, True)
+        assert_same(got, want, FIELDS, "custom")
+        assert got.aln_a == sa and got.aln_b == sb
+
+
+def test_graph_replay_and_device_resident_batch():
+    ps = random_pairs(5, 3000, 20, 500)
+    want = oracle_batch(ps, False, O.MODE_SCORE)
+    with A.Batch(ps, output="score", use_graph=True) as b:
+        for _ in range(3):
+            b.run()
+            got = b.results()
+            assert_same(got, want, ("score",), "graph replay")
+        st = b.stats()
+        assert st["cells"] == ps.cells and st["pairs"] == len(ps) and st["device_ms"] > 0
+
+
+def test_plain_equals_batch():
+    ps = random_pairs(21, 40, 0, 900)
+    bat = gpu_batch(ps, True, "alignment")
+    for k in range(len(ps)):
+        a, b = ps.pair(k)
+        r = A.align_pair(a, b, mode="local", output="alignment")
+        assert (r.score, r.aln_a, r.aln_b, r.a_begin, r.b_begin) == (
+            int(bat.table["score"][k]), bat.aln_a[k], bat.aln_b[k], int(bat.table["a_begin"][k]),
+            int(bat.table["b_begin"][k]))

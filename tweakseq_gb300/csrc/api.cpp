@@ -1,0 +1,163 @@
+// api.cpp -- the extern "C" entry points declared in include/tweakseq_gb300.h.
+#include <cstdlib>
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <new>
+
+#include "engine.h"
+
+namespace {
+
+// One cached engine object per host thread and device, so that repeated
+// plain or batch calls reuse their device buffers instead of allocating.
+struct ThreadCache {
+  std::unique_ptr<tsq_batch> pair_engine;
+  std::unique_ptr<tsq_batch> batch_engine;
+  int pair_dev = -1, batch_dev = -1;
+};
+
+ThreadCache &cache() {
+  thread_local ThreadCache c;
+  return c;
+}
+
+int current_device(const tsq_batch_opts *opts, int *dev) {
+  if (opts && opts->device >= 0) {
+    *dev = opts->device;
+    return TSQ_OK;
+  }
+  const cudaError_t e = cudaGetDevice(dev);
+  return e == cudaSuccess ? TSQ_OK : TSQ_E_CUDA;
+}
+
+template <class F>
+int guarded(F &&f) {
+  try {
+    return f();
+  } catch (const std::bad_alloc &) {
+    return TSQ_E_NOMEM;
+  } catch (...) {
+    return TSQ_E_CUDA;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int tsq_version(int32_t *abi_version, const char **build) {
+  if (abi_version) *abi_version = TSQ_ABI_VERSION;
+  if (build) *build = "tweakseq_gb300 sm_103a int32 group-striped Gotoh fill + traceback";
+  return TSQ_OK;
+}
+
+void tsq_result_free(tsq_result *r) {
+  if (!r) return;
+  std::free(r->aln_a);
+  std::free(r->aln_b);
+  r->aln_a = r->aln_b = nullptr;
+}
+
+void tsq_results_free(tsq_result *r, int64_t n) {
+  if (!r) return;
+  for (int64_t k = 0; k < n; ++k) tsq_result_free(&r[k]);
+}
+
+int tsq_align_pair(const uint8_t *a, int32_t la, const uint8_t *b, int32_t lb, const tsq_params *p,
+                   tsq_result *out) {
+  return guarded([&]() -> int {
+    if (!out || !p || la < 0 || lb < 0 || (la > 0 && !a) || (lb > 0 && !b)) return TSQ_E_INVALID_ARG;
+    std::memset(out, 0, sizeof(*out));
+    int dev = 0;
+    if (current_device(nullptr, &dev)) return TSQ_E_CUDA;
+    ThreadCache &c = cache();
+    if (!c.pair_engine || c.pair_dev != dev) {
+      c.pair_engine.reset(new tsq_batch());
+      c.pair_dev = dev;
+    }
+    // The pair's residues go up as one buffer: a then b.
+    std::unique_ptr<uint8_t[]> buf(new uint8_t[size_t(la) + size_t(lb) + 1]);
+    if (la) std::memcpy(buf.get(), a, size_t(la));
+    if (lb) std::memcpy(buf.get() + la, b, size_t(lb));
+    tsq_pair_desc d{0, la, la, lb};
+    tsq_batch *e = c.pair_engine.get();
+    int rc = tsq::batch_plan(e, buf.get(), int64_t(la) + lb, &d, 1, p, nullptr, true);
+    if (rc) return rc;
+    if ((rc = tsq::batch_run_async(e))) return rc;
+    if ((rc = tsq::batch_sync(e))) return rc;
+    return tsq::batch_results(e, out);
+  });
+}
+
+int tsq_align_batch(const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *pairs, int64_t n,
+                    const tsq_params *p, const tsq_batch_opts *opts, tsq_result *out) {
+  return guarded([&]() -> int {
+    if (n > 0 && !out) return TSQ_E_INVALID_ARG;
+    int dev = 0;
+    if (current_device(opts, &dev)) return TSQ_E_CUDA;
+    ThreadCache &c = cache();
+    if (!c.batch_engine || c.batch_dev != dev) {
+      c.batch_engine.reset(new tsq_batch());
+      c.batch_dev = dev;
+    }
+    tsq_batch *e = c.batch_engine.get();
+    int rc = tsq::batch_plan(e, seqs, seqs_len, pairs, n, p, opts, false);
+    if (rc) return rc;
+    if ((rc = tsq::batch_run_async(e))) return rc;
+    if ((rc = tsq::batch_sync(e))) return rc;
+    return tsq::batch_results(e, out);
+  });
+}
+
+int tsq_batch_create(const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *pairs, int64_t n,
+                     const tsq_params *p, const tsq_batch_opts *opts, tsq_batch **out) {
+  return guarded([&]() -> int {
+    if (!out) return TSQ_E_INVALID_ARG;
+    *out = nullptr;
+    std::unique_ptr<tsq_batch> b(new tsq_batch());
+    const int rc = tsq::batch_plan(b.get(), seqs, seqs_len, pairs, n, p, opts, false);
+    if (rc) return rc;
+    *out = b.release();
+    return TSQ_OK;
+  });
+}
+
+int tsq_batch_run(tsq_batch *b) {
+  return guarded([&]() -> int {
+    const int rc = tsq::batch_run_async(b);
+    return rc ? rc : tsq::batch_sync(b);
+  });
+}
+
+int tsq_batch_run_async(tsq_batch *b) {
+  return guarded([&]() -> int { return tsq::batch_run_async(b); });
+}
+
+int tsq_batch_sync(tsq_batch *b) {
+  return guarded([&]() -> int { return tsq::batch_sync(b); });
+}
+
+int tsq_batch_results(tsq_batch *b, tsq_result *out) {
+  return guarded([&]() -> int { return tsq::batch_results(b, out); });
+}
+
+int tsq_batch_get_stats(const tsq_batch *b, tsq_batch_stats *st) {
+  if (!b || !st) return TSQ_E_INVALID_ARG;
+  *st = b->stats;
+  return TSQ_OK;
+}
+
+int tsq_batch_stream(const tsq_batch *b, void **stream) {
+  if (!b || !stream) return TSQ_E_INVALID_ARG;
+  *stream = static_cast<void *>(b->stream);
+  return TSQ_OK;
+}
+
+void tsq_batch_destroy(tsq_batch *b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  delete b;
+}
+
+}  // extern "C"

@@ -1,0 +1,451 @@
+// engine.cpp -- planning and running batches of pairs on one GPU.
+//
+// A plan buckets the pairs by kernel shape (lanes per pair G, rows per lane
+// R), sorts every bucket by (bands, columns) descending so the groups of a
+// warp get pairs of nearly the same shape and the longest pairs start first,
+// and turns each bucket into one persistent launch whose warps pull pairs
+// from an atomic counter.  A run is: reset the counters, encode the residues,
+// one fill launch per bucket, and (alignment output) the traceback walk.
+// The run can be captured once as a CUDA graph and replayed.
+#include "engine.h"
+
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <numeric>
+
+namespace tsq {
+
+cudaError_t DevBuf::ensure(size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (bytes <= cap) return cudaSuccess;
+  release();
+  const size_t want = (bytes + 255) & ~size_t(255);
+  cudaError_t e = cudaMalloc(&p, want);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    return e;
+  }
+  cap = want;
+  return cudaSuccess;
+}
+
+void DevBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+}
+
+cudaError_t PinBuf::ensure(size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (bytes <= cap) return cudaSuccess;
+  release();
+  const size_t want = (bytes + 4095) & ~size_t(4095);
+  cudaError_t e = cudaMallocHost(&p, want);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    return e;
+  }
+  cap = want;
+  return cudaSuccess;
+}
+
+void PinBuf::release() {
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  cap = 0;
+}
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return TSQ_OK;
+  if (e == cudaErrorMemoryAllocation) return TSQ_E_NOMEM;
+  return TSQ_E_CUDA;
+}
+
+#define TSQ_TRY(expr)                          \
+  do {                                         \
+    const cudaError_t e_ = (expr);             \
+    if (e_ != cudaSuccess) return cuda_status(e_); \
+  } while (0)
+
+namespace {
+
+int pow2ceil(int64_t x) {
+  int v = 1;
+  while (v < x && v < (1 << 30)) v <<= 1;
+  return v;
+}
+
+constexpr int kR = 8;
+// Longest sequence the int32 kernels take: coordinates travel in 20 bits.
+constexpr int64_t kMaxLen = (1 << 20) - 1;
+
+}  // namespace
+
+Shape ShapeChooser::pick(int m, int n) const {
+  // Enough warps to fill every SM about 24 deep ...
+  const int64_t target_warps = int64_t(sms) * 24;
+  int g_occ = npairs > 0 ? pow2ceil((target_warps * 32 + npairs - 1) / npairs) : 32;
+  g_occ = std::max(4, std::min(32, g_occ));
+  Shape sh{};
+  if (use_table && tune_table_pick(out_mode, m, n, &sh) && shape_supported(sh, out_mode, local)) {
+    if (!tune_forced() && sh.G < g_occ) {
+      Shape wider = sh;
+      wider.G = g_occ;
+      if (shape_supported(wider, out_mode, local)) sh = wider;
+    }
+    return sh;
+  }
+  // ... and no more lanes per pair than its rows can use.
+  sh.R = kR;
+  sh.i16 = 0;
+  const int rows_cap = pow2ceil((m + kR - 1) / kR);
+  sh.G = std::max(4, std::min(g_occ, rows_cap));
+  (void)n;
+  return sh;
+}
+
+}  // namespace tsq
+
+tsq_batch::~tsq_batch() {
+  if (gexec) cudaGraphExecDestroy(gexec);
+  if (graph) cudaGraphDestroy(graph);
+  for (auto &e : ev)
+    if (e) cudaEventDestroy(e);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+namespace tsq {
+
+int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *pairs, int64_t n,
+               const tsq_params *p, const tsq_batch_opts *opts, bool plain) {
+  if (!b || !p || n < 0 || seqs_len < 0) return TSQ_E_INVALID_ARG;
+  if (n > 0 && !pairs) return TSQ_E_INVALID_ARG;
+  if (seqs_len > 0 && !seqs) return TSQ_E_INVALID_ARG;
+  if (n > INT32_MAX / 2) return TSQ_E_TOO_LARGE;
+  if (p->gap_open < 0 || p->gap_extend < 0 || p->gap_open > 1000000 || p->gap_extend > 1000000)
+    return TSQ_E_INVALID_ARG;
+  if (p->mode != TSQ_GLOBAL && p->mode != TSQ_LOCAL) return TSQ_E_INVALID_ARG;
+  if (p->output < TSQ_OUT_SCORE || p->output > TSQ_OUT_ALIGNMENT) return TSQ_E_INVALID_ARG;
+  if (p->lane < TSQ_LANE_AUTO || p->lane > TSQ_LANE_I32) return TSQ_E_INVALID_ARG;
+  Scheme sc;
+  int rc = build_scheme(p, &sc);
+  if (rc) return rc;
+
+  int dev = opts && opts->device >= 0 ? opts->device : -1;
+  if (dev < 0) TSQ_TRY(cudaGetDevice(&dev));
+  TSQ_TRY(cudaSetDevice(dev));
+  int sms = 0;
+  TSQ_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+
+  // A replanned object drops its old graph.
+  if (b->gexec) {
+    cudaGraphExecDestroy(b->gexec);
+    b->gexec = nullptr;
+  }
+  if (b->graph) {
+    cudaGraphDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  if (b->stream && b->device != dev) {
+    cudaStreamDestroy(b->stream);
+    b->stream = nullptr;
+  }
+  b->device = dev;
+  if (!b->stream) TSQ_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  for (auto &e : b->ev)
+    if (!e) TSQ_TRY(cudaEventCreate(&e));
+
+  b->scheme = sc;
+  b->params = *p;
+  b->out_mode = p->output == TSQ_OUT_ALIGNMENT ? kOutTrace : (p->output == TSQ_OUT_IDENTITY ? kOutIdent : kOutScore);
+  b->local = p->mode == TSQ_LOCAL;
+  b->use_graph = opts ? opts->use_graph != 0 : false;
+  b->autotune = opts ? opts->autotune != 0 : false;
+  b->n = n;
+  b->seqs_len = seqs_len;
+  b->has_run = false;
+  b->stats = tsq_batch_stats{};
+
+  // Validate the pair table and the value range the int32 kernels assume:
+  // every H, E, F stays above -(3*open + (m+n+1)*ext + 128), which must be
+  // far from the kernels' "minus infinity" (-2^29).
+  b->pairs_h.resize(size_t(n));
+  int64_t cells = 0;
+  int32_t max_n = 0;
+  for (int64_t k = 0; k < n; ++k) {
+    const tsq_pair_desc &d = pairs[k];
+    if (d.a_len < 0 || d.b_len < 0 || d.a_off < 0 || d.b_off < 0) return TSQ_E_INVALID_ARG;
+    if (d.a_off > seqs_len - d.a_len || d.b_off > seqs_len - d.b_len) return TSQ_E_INVALID_ARG;
+    if (d.a_len > kMaxLen || d.b_len > kMaxLen) return TSQ_E_TOO_LARGE;
+    const int64_t low = 3 * int64_t(p->gap_open) + (int64_t(d.a_len) + d.b_len + 1) * p->gap_extend + 128;
+    if (low >= (int64_t(1) << 28)) return TSQ_E_TOO_LARGE;
+    if (b->out_mode == kOutIdent && int64_t(d.a_len) + d.b_len > 65535) return TSQ_E_TOO_LARGE;
+    // Local maxima travel in 24 bits of the reduction key.
+    if (p->mode == TSQ_LOCAL && int64_t(std::max(sc.max_score, 0)) * std::min(d.a_len, d.b_len) >= (1 << 23))
+      return TSQ_E_TOO_LARGE;
+    b->pairs_h[size_t(k)] = PairDev{d.a_off, d.b_off, d.a_len, d.b_len};
+    cells += int64_t(d.a_len) * d.b_len;
+    max_n = std::max(max_n, d.b_len);
+  }
+  b->cells = cells;
+
+  // ---- shapes and buckets ----------------------------------------------
+  ShapeChooser ch;
+  ch.out_mode = b->out_mode;
+  ch.local = b->local;
+  ch.sms = sms;
+  ch.npairs = plain ? 1 : n;
+  ch.use_table = b->autotune && tune_table_loaded();
+  std::vector<int32_t> gsel(static_cast<size_t>(n));
+  std::vector<int32_t> rsel(static_cast<size_t>(n));
+  std::vector<int32_t> order(static_cast<size_t>(n));
+  for (int64_t k = 0; k < n; ++k) {
+    const Shape s = ch.pick(b->pairs_h[size_t(k)].a_len, b->pairs_h[size_t(k)].b_len);
+    if (!shape_supported(s, b->out_mode, b->local)) return TSQ_E_INVALID_ARG;
+    gsel[size_t(k)] = s.G;
+    rsel[size_t(k)] = s.R;
+    order[size_t(k)] = int32_t(k);
+  }
+  auto bands = [&](int32_t k) {
+    const int P = gsel[size_t(k)] * rsel[size_t(k)];
+    return (b->pairs_h[size_t(k)].a_len + P - 1) / P;
+  };
+  std::sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+    if (gsel[size_t(x)] != gsel[size_t(y)]) return gsel[size_t(x)] < gsel[size_t(y)];
+    if (rsel[size_t(x)] != rsel[size_t(y)]) return rsel[size_t(x)] < rsel[size_t(y)];
+    const int bx = bands(x), by = bands(y);
+    if (bx != by) return bx > by;
+    const int nx = b->pairs_h[size_t(x)].b_len, ny = b->pairs_h[size_t(y)].b_len;
+    if (nx != ny) return nx > ny;
+    return x < y;
+  });
+  b->launches.clear();
+  const int BW = b->out_mode == kOutIdent ? 4 : 2;
+  int64_t bnd_total = 0;
+  for (int64_t s = 0; s < n;) {
+    int64_t e = s;
+    const int G = gsel[size_t(order[size_t(s)])], R = rsel[size_t(order[size_t(s)])];
+    int32_t cols = 1;
+    while (e < n && gsel[size_t(order[size_t(e)])] == G && rsel[size_t(order[size_t(e)])] == R) {
+      cols = std::max(cols, b->pairs_h[size_t(order[size_t(e)])].b_len + 1);
+      ++e;
+    }
+    Launch L;
+    L.sh = Shape{G, R, 0};
+    L.task_begin = int32_t(s);
+    L.n_tasks = int32_t(e - s);
+    const int max_blocks = fill_blocks(L.sh, b->out_mode, b->local);
+    if (max_blocks <= 0) return TSQ_E_CUDA;
+    const int64_t needed = (int64_t(L.n_tasks) * G + fill_threads() - 1) / fill_threads();
+    L.blocks = int32_t(std::max<int64_t>(1, std::min<int64_t>(max_blocks, needed)));
+    L.slots = L.blocks * (fill_threads() / G);
+    L.bnd_cols = cols;
+    L.bnd_offset = bnd_total;
+    bnd_total += int64_t(L.slots) * BW * cols;
+    b->launches.push_back(L);
+    s = e;
+  }
+  b->stats.pairs = n;
+  b->stats.cells = cells;
+  b->stats.launches = int32_t(b->launches.size()) + 1 + (b->out_mode == kOutTrace ? 1 : 0);
+  b->stats.buckets = int32_t(b->launches.size());
+
+  // ---- traceback layout ----------------------------------------------------
+  std::vector<int64_t> ploff;
+  b->aln_off_h.clear();
+  b->aln_bytes = 0;
+  int64_t plane_total = 0;
+  if (b->out_mode == kOutTrace) {
+    ploff.resize(size_t(n));
+    b->aln_off_h.resize(size_t(n));
+    for (int64_t k = 0; k < n; ++k) {
+      const PairDev &pd = b->pairs_h[size_t(k)];
+      ploff[size_t(k)] = plane_total;
+      plane_total += plane_bytes(pd.a_len, pd.b_len, Shape{gsel[size_t(k)], rsel[size_t(k)], 0});
+      b->aln_off_h[size_t(k)] = b->aln_bytes;
+      b->aln_bytes += 2 * (int64_t(pd.a_len) + pd.b_len);
+    }
+  }
+
+  // ---- device buffers and uploads -------------------------------------------
+  uint8_t lut[256];
+  build_lut(sc, lut);
+  TSQ_TRY(b->seqs.ensure(size_t(seqs_len) + 16));
+  TSQ_TRY(b->codes.ensure(size_t(seqs_len) + 16));
+  TSQ_TRY(b->pairs.ensure(sizeof(PairDev) * size_t(n)));
+  TSQ_TRY(b->tasks.ensure(sizeof(int32_t) * size_t(n)));
+  TSQ_TRY(b->res.ensure(sizeof(ResultDev) * size_t(n)));
+  TSQ_TRY(b->bnd.ensure(sizeof(int32_t) * size_t(bnd_total)));
+  TSQ_TRY(b->counters.ensure(sizeof(int32_t) * (b->launches.size() + 1)));
+  TSQ_TRY(b->lut.ensure(256));
+  TSQ_TRY(b->matrix.ensure(kLetters * kLetters));
+  TSQ_TRY(b->res_h.ensure(sizeof(ResultDev) * size_t(n)));
+  if (b->out_mode == kOutTrace) {
+    TSQ_TRY(b->planes.ensure(size_t(plane_total)));
+    TSQ_TRY(b->plane_off.ensure(sizeof(int64_t) * size_t(n)));
+    TSQ_TRY(b->aln.ensure(size_t(b->aln_bytes)));
+    TSQ_TRY(b->aln_off.ensure(sizeof(int64_t) * size_t(n)));
+    TSQ_TRY(b->shape_g.ensure(sizeof(int32_t) * size_t(n)));
+    TSQ_TRY(b->shape_r.ensure(sizeof(int32_t) * size_t(n)));
+    TSQ_TRY(b->aln_h.ensure(size_t(b->aln_bytes)));
+  }
+  cudaStream_t st = b->stream;
+  if (seqs_len > 0) TSQ_TRY(cudaMemcpyAsync(b->seqs.p, seqs, size_t(seqs_len), cudaMemcpyHostToDevice, st));
+  if (n > 0) {
+    TSQ_TRY(cudaMemcpyAsync(b->pairs.p, b->pairs_h.data(), sizeof(PairDev) * size_t(n), cudaMemcpyHostToDevice, st));
+    TSQ_TRY(cudaMemcpyAsync(b->tasks.p, order.data(), sizeof(int32_t) * size_t(n), cudaMemcpyHostToDevice, st));
+  }
+  TSQ_TRY(cudaMemcpyAsync(b->lut.p, lut, 256, cudaMemcpyHostToDevice, st));
+  TSQ_TRY(cudaMemcpyAsync(b->matrix.p, sc.score, kLetters * kLetters, cudaMemcpyHostToDevice, st));
+  if (b->out_mode == kOutTrace && n > 0) {
+    TSQ_TRY(cudaMemcpyAsync(b->plane_off.p, ploff.data(), sizeof(int64_t) * size_t(n), cudaMemcpyHostToDevice, st));
+    TSQ_TRY(cudaMemcpyAsync(b->aln_off.p, b->aln_off_h.data(), sizeof(int64_t) * size_t(n), cudaMemcpyHostToDevice,
+                            st));
+    TSQ_TRY(cudaMemcpyAsync(b->shape_g.p, gsel.data(), sizeof(int32_t) * size_t(n), cudaMemcpyHostToDevice, st));
+    TSQ_TRY(cudaMemcpyAsync(b->shape_r.p, rsel.data(), sizeof(int32_t) * size_t(n), cudaMemcpyHostToDevice, st));
+  }
+  // The host vectors above go out of scope: wait for the copies.
+  TSQ_TRY(cudaStreamSynchronize(st));
+  return TSQ_OK;
+}
+
+namespace {
+
+int enqueue_run(tsq_batch *b) {
+  cudaStream_t st = b->stream;
+  const int nl = int(b->launches.size());
+  TSQ_TRY(cudaMemsetAsync(b->counters.p, 0, sizeof(int32_t) * (size_t(nl) + 1), st));
+  TSQ_TRY(cudaEventRecord(b->ev[0], st));
+  TSQ_TRY(launch_encode(b->seqs.as<uint8_t>(), b->seqs_len, b->lut.as<uint8_t>(), b->codes.as<uint8_t>(), st));
+  TSQ_TRY(cudaEventRecord(b->ev[1], st));
+  for (int l = 0; l < nl; ++l) {
+    const Launch &L = b->launches[size_t(l)];
+    FillArgs a{};
+    a.codes = b->codes.as<uint8_t>();
+    a.pairs = b->pairs.as<PairDev>();
+    a.tasks = b->tasks.as<int32_t>() + L.task_begin;
+    a.n_tasks = L.n_tasks;
+    a.counter = b->counters.as<int32_t>() + l;
+    a.matrix = b->matrix.as<int8_t>();
+    a.gap_open = b->params.gap_open;
+    a.gap_extend = b->params.gap_extend;
+    a.res = b->res.as<ResultDev>();
+    a.bnd = b->bnd.as<int32_t>() + L.bnd_offset;
+    a.bnd_cols = L.bnd_cols;
+    a.n_slots = L.slots;
+    a.planes = b->planes.as<uint8_t>();
+    a.plane_off = b->plane_off.as<int64_t>();
+    a.overflow = nullptr;
+    TSQ_TRY(launch_fill(L.sh, b->out_mode, b->local, a, L.blocks, st));
+  }
+  TSQ_TRY(cudaEventRecord(b->ev[2], st));
+  if (b->out_mode == kOutTrace) {
+    WalkArgs w{};
+    w.seqs = b->seqs.as<uint8_t>();
+    w.codes = b->codes.as<uint8_t>();
+    w.pairs = b->pairs.as<PairDev>();
+    w.tasks = b->tasks.as<int32_t>();
+    w.n_tasks = int32_t(b->n);
+    w.planes = b->planes.as<uint8_t>();
+    w.plane_off = b->plane_off.as<int64_t>();
+    w.shape_G = b->shape_g.as<int32_t>();
+    w.shape_R = b->shape_r.as<int32_t>();
+    w.local = b->local ? 1 : 0;
+    w.res = b->res.as<ResultDev>();
+    w.aln = b->aln.as<char>();
+    w.aln_off = b->aln_off.as<int64_t>();
+    TSQ_TRY(launch_walk(w, st));
+  }
+  TSQ_TRY(cudaEventRecord(b->ev[3], st));
+  return TSQ_OK;
+}
+
+}  // namespace
+
+int batch_run_async(tsq_batch *b) {
+  if (!b) return TSQ_E_INVALID_ARG;
+  TSQ_TRY(cudaSetDevice(b->device));
+  if (!b->use_graph) {
+    const int rc = enqueue_run(b);
+    if (rc) return rc;
+  } else {
+    if (!b->gexec) {
+      TSQ_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      const int rc = enqueue_run(b);
+      cudaGraph_t g = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      TSQ_TRY(e);
+      b->graph = g;
+      TSQ_TRY(cudaGraphInstantiate(&b->gexec, b->graph, 0));
+    }
+    TSQ_TRY(cudaGraphLaunch(b->gexec, b->stream));
+  }
+  b->has_run = true;
+  return TSQ_OK;
+}
+
+int batch_sync(tsq_batch *b) {
+  if (!b) return TSQ_E_INVALID_ARG;
+  TSQ_TRY(cudaStreamSynchronize(b->stream));
+  float total = 0.f, fill = 0.f;
+  if (b->has_run && cudaEventElapsedTime(&total, b->ev[0], b->ev[3]) == cudaSuccess) b->stats.device_ms = total;
+  if (b->has_run && cudaEventElapsedTime(&fill, b->ev[1], b->ev[2]) == cudaSuccess) b->stats.fill_ms = fill;
+  return TSQ_OK;
+}
+
+int batch_results(tsq_batch *b, tsq_result *out) {
+  if (!b || (b->n > 0 && !out)) return TSQ_E_INVALID_ARG;
+  if (!b->has_run) return TSQ_E_INVALID_ARG;
+  cudaStream_t st = b->stream;
+  if (b->n > 0)
+    TSQ_TRY(cudaMemcpyAsync(b->res_h.p, b->res.p, sizeof(ResultDev) * size_t(b->n), cudaMemcpyDeviceToHost, st));
+  if (b->out_mode == kOutTrace && b->aln_bytes > 0)
+    TSQ_TRY(cudaMemcpyAsync(b->aln_h.p, b->aln.p, size_t(b->aln_bytes), cudaMemcpyDeviceToHost, st));
+  TSQ_TRY(cudaStreamSynchronize(st));
+  const ResultDev *r = b->res_h.as<ResultDev>();
+  int rc = TSQ_OK;
+  for (int64_t k = 0; k < b->n; ++k) {
+    tsq_result &o = out[k];
+    const ResultDev &d = r[k];
+    o.score = d.score;
+    o.a_begin = d.a_begin;
+    o.a_end = d.a_end;
+    o.b_begin = d.b_begin;
+    o.b_end = d.b_end;
+    o.n_ident = d.n_ident;
+    o.n_cols = d.n_cols;
+    o.status = d.status;
+    o.aln_a = o.aln_b = nullptr;
+    if (d.status != TSQ_OK) {
+      rc = TSQ_E_INVALID_RESIDUE;
+      continue;
+    }
+    if (b->out_mode == kOutTrace) {
+      const PairDev &pd = b->pairs_h[size_t(k)];
+      const int64_t cap = int64_t(pd.a_len) + pd.b_len;
+      const int64_t L = d.n_cols;
+      if (L < 0 || L > cap) return TSQ_E_CUDA;
+      const char *base = b->aln_h.as<char>() + b->aln_off_h[size_t(k)];
+      o.aln_a = static_cast<char *>(std::malloc(size_t(L) + 1));
+      o.aln_b = static_cast<char *>(std::malloc(size_t(L) + 1));
+      if (!o.aln_a || !o.aln_b) {
+        std::free(o.aln_a);
+        std::free(o.aln_b);
+        o.aln_a = o.aln_b = nullptr;
+        return TSQ_E_NOMEM;
+      }
+      std::memcpy(o.aln_a, base + cap - L, size_t(L));
+      std::memcpy(o.aln_b, base + 2 * cap - L, size_t(L));
+      o.aln_a[L] = 0;
+      o.aln_b[L] = 0;
+    }
+  }
+  return rc;
+}
+
+}  // namespace tsq

@@ -1,0 +1,108 @@
+// engine.h -- host-side batch engine behind the C ABI.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "tsq_internal.h"
+
+namespace tsq {
+
+// Device buffer that only grows; reused across plans of the same object.
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes);
+  void release();
+  template <class T>
+  T *as() const {
+    return static_cast<T *>(p);
+  }
+  ~DevBuf() { release(); }
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+};
+
+// Page-locked host buffer (for results coming back asynchronously).
+struct PinBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes);
+  void release();
+  template <class T>
+  T *as() const {
+    return static_cast<T *>(p);
+  }
+  ~PinBuf() { release(); }
+  PinBuf() = default;
+  PinBuf(const PinBuf &) = delete;
+  PinBuf &operator=(const PinBuf &) = delete;
+};
+
+// One persistent fill launch over a bucket of pairs of one kernel shape.
+struct Launch {
+  Shape sh;
+  int32_t task_begin = 0, n_tasks = 0;
+  int32_t blocks = 0;
+  int32_t bnd_cols = 0;
+  int64_t bnd_offset = 0;  // int32 elements into the boundary scratch
+  int32_t slots = 0;
+};
+
+// Kernel-shape choice.  A tuned table (lengths -> shape) overrides the
+// occupancy heuristic when loaded and enabled.
+struct ShapeChooser {
+  int out_mode = kOutScore;
+  bool local = false;
+  int sms = 152;
+  int64_t npairs = 0;
+  bool use_table = false;
+  Shape pick(int m, int n) const;
+};
+
+bool tune_table_loaded();
+bool tune_forced();
+bool tune_table_pick(int out_mode, int m, int n, Shape *sh);
+
+}  // namespace tsq
+
+struct tsq_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  tsq::Scheme scheme{};
+  tsq_params params{};
+  int out_mode = tsq::kOutScore;
+  bool local = false;
+  bool use_graph = false;
+  bool autotune = false;
+  int64_t n = 0;
+  int64_t seqs_len = 0;
+  int64_t cells = 0;
+  std::vector<tsq::PairDev> pairs_h;
+  std::vector<tsq::Launch> launches;
+  std::vector<int64_t> aln_off_h;
+  int64_t aln_bytes = 0;
+  bool has_run = false;
+
+  tsq::DevBuf seqs, codes, pairs, tasks, res, bnd, planes, plane_off, aln, aln_off, shape_g, shape_r, counters,
+      lut, matrix;
+  tsq::PinBuf res_h, aln_h;
+
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  tsq_batch_stats stats{};
+
+  ~tsq_batch();
+};
+
+namespace tsq {
+int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *pairs, int64_t n,
+               const tsq_params *p, const tsq_batch_opts *opts, bool plain);
+int batch_run_async(tsq_batch *b);
+int batch_sync(tsq_batch *b);
+int batch_results(tsq_batch *b, tsq_result *out);
+int cuda_status(cudaError_t e);
+}  // namespace tsq

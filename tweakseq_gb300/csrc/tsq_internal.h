@@ -1,0 +1,118 @@
+// tsq_internal.h -- shared declarations of the GB300 alignment library.
+//
+// Device data layout (all in HBM, one allocation pool per context):
+//   codes      uint8 per residue: 'A'..'Z' -> 0..25 when the scheme accepts
+//              the letter, kBadCode otherwise (converted once per batch).
+//   pairs      PairDev per pair (offsets into codes, lengths).
+//   tasks      int32 pair ids of one launch, sorted so that the groups of a
+//              warp get pairs of nearly the same shape.
+//   results    ResultDev per pair.
+//   boundary   per group slot, two rows of (H, F) of max_n + 1 columns: the
+//              bottom row of one band of rows is the top row of the next.
+//   planes     traceback nibbles (TB mode), diagonal-major per band so the
+//              lanes of a group store one contiguous run per step.
+#pragma once
+
+#include <cstdint>
+#include <cstddef>
+
+#include <cuda_runtime.h>
+
+#include "../../include/tweakseq_gb300.h"
+
+namespace tsq {
+
+constexpr uint8_t kBadCode = 0xFF;
+constexpr int kLetters = 26;
+constexpr int32_t kNegInf = -(1 << 29);  // "minus infinity" for int32 E/F
+
+// Output modes of the fill kernels.
+enum : int { kOutScore = 0, kOutIdent = 1, kOutTrace = 2 };
+// Traceback nibble: bits 0-1 H source, bit 2 E opened, bit 3 F opened.
+enum : int { kDirDiag = 0, kDirE = 1, kDirF = 2, kDirStop = 3 };
+
+struct Scheme {
+  int8_t score[kLetters][kLetters];
+  uint8_t valid[kLetters];
+  int32_t max_score, min_score;
+  bool symmetric;
+};
+
+struct PairDev {
+  int64_t a_off, b_off;
+  int32_t a_len, b_len;
+};
+
+struct ResultDev {
+  int32_t score;
+  int32_t a_begin, a_end, b_begin, b_end;
+  int32_t n_ident, n_cols;
+  int32_t status;
+};
+
+// Kernel shape of the group-striped fill: G lanes per pair, R rows per lane,
+// int32 or int16x2 values.
+struct Shape {
+  int G, R, i16;
+};
+
+struct FillArgs {
+  const uint8_t *codes;
+  const PairDev *pairs;
+  const int32_t *tasks;
+  int32_t n_tasks;
+  int32_t *counter;  // work-queue head, zero before the launch
+  const int8_t *matrix;  // 26*26 device copy of the scheme
+  int32_t gap_open, gap_extend;
+  ResultDev *res;
+  int32_t *bnd;       // boundary scratch
+  int32_t bnd_cols;   // max_n + 1 over the launch
+  int32_t n_slots;    // number of group slots the scratch holds
+  uint8_t *planes;    // TB planes (kOutTrace)
+  const int64_t *plane_off;  // byte offset of each pair's planes
+  int32_t *overflow;  // int16: per pair flag, set when a lane saturated
+};
+
+struct WalkArgs {
+  const uint8_t *seqs;  // ASCII residues (for the emitted strings)
+  const uint8_t *codes;
+  const PairDev *pairs;
+  const int32_t *tasks;
+  int32_t n_tasks;
+  const uint8_t *planes;
+  const int64_t *plane_off;
+  const int32_t *shape_G;  // per pair: the G and R its planes were written with
+  const int32_t *shape_R;
+  int32_t local;
+  ResultDev *res;
+  char *aln;                 // per pair: 2 * cap bytes (a row then b row)
+  const int64_t *aln_off;
+};
+
+// Host-side helpers (scheme.cpp).
+int build_scheme(const tsq_params *p, Scheme *out);
+void build_lut(const Scheme &s, uint8_t lut[256]);
+
+// Kernel launchers (fill_kernels.cu, walk_kernel.cu, encode in batch.cu).
+// Returns the number of thread blocks a persistent launch of this shape uses.
+int fill_blocks(const Shape &sh, int out_mode, bool local);
+size_t fill_smem_bytes(const Shape &sh);
+int fill_threads();
+cudaError_t launch_fill(const Shape &sh, int out_mode, bool local, const FillArgs &a, int blocks,
+                        cudaStream_t st);
+bool shape_supported(const Shape &sh, int out_mode, bool local);
+cudaError_t launch_walk(const WalkArgs &a, cudaStream_t st);
+cudaError_t launch_encode(const uint8_t *seqs, int64_t len, const uint8_t *lut_dev, uint8_t *codes,
+                          cudaStream_t st);
+
+// Bytes of traceback planes a pair needs under a shape.
+inline int64_t plane_bytes(int m, int n, const Shape &sh) {
+  if (m <= 0 || n <= 0) return 0;
+  const int64_t P = (int64_t)sh.G * sh.R;
+  const int64_t passes = (m + P - 1) / P;
+  const int64_t entry = sh.R / 2;  // R nibbles per lane per step
+  int64_t b = passes * (int64_t)(n + sh.G - 1) * sh.G * entry;
+  return (b + 15) & ~int64_t(15);
+}
+
+}  // namespace tsq

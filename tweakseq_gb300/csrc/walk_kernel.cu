@@ -1,0 +1,188 @@
+// walk_kernel.cu -- traceback walker and residue encoder.
+//
+// The walker follows the 4-bit direction planes written by the fill from the
+// end cell back to the start, exactly as the CPU oracle's walk does (state
+// machine over H, E and F; E and F runs end where the "opened" bit is set;
+// global rows/columns 0 are single gap runs; local stops on a STOP cell or
+// row/column 0).  It emits the two gapped rows backwards into the pair's
+// output slot, so the aligned strings end at slot + cap and start at
+// slot + cap - n_cols, and records identity, column count and the begin
+// coordinates.
+#include <algorithm>
+
+#include "tsq_internal.h"
+
+namespace tsq {
+namespace {
+
+struct PlaneReader {
+  const uint8_t *base;
+  int n, G, R;
+  __device__ int nib(int i, int j) const {
+    // (i, j) are 1-based cell coordinates with i, j >= 1.
+    const int P = G * R;
+    const int row0 = i - 1;
+    const int pass = row0 / P;
+    const int w = row0 - pass * P;
+    const int t = w / R;
+    const int r = w - t * R;
+    const int s = (j - 1) + t;
+    const int64_t entry = ((int64_t)pass * (n + G - 1) + s) * G + t;
+    const int64_t byte = entry * (R / 2) + (r >> 1);
+    return (base[byte] >> ((r & 1) * 4)) & 15;
+  }
+};
+
+__global__ void walk_kernel(const WalkArgs A) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= A.n_tasks) return;
+  const int p = A.tasks[k];
+  const PairDev pr = A.pairs[p];
+  ResultDev &res = A.res[p];
+  if (res.status != TSQ_OK) return;
+  const int m = pr.a_len, n = pr.b_len;
+  const uint8_t *a = A.seqs + pr.a_off;
+  const uint8_t *b = A.seqs + pr.b_off;
+  const int64_t cap = (int64_t)m + n;
+  char *out_a = A.aln + A.aln_off[p];
+  char *out_b = out_a + cap;
+  PlaneReader pl{A.planes + A.plane_off[p], n, A.shape_G[p], A.shape_R[p]};
+
+  int i, j;
+  if (A.local) {
+    if (res.score <= 0) {
+      res.a_begin = res.a_end = res.b_begin = res.b_end = 0;
+      res.n_ident = res.n_cols = 0;
+      return;
+    }
+    i = res.a_end;
+    j = res.b_end;
+  } else {
+    i = m;
+    j = n;
+  }
+  int state = 0;  // 0 = H, 1 = E, 2 = F
+  int64_t L = 0;
+  int ident = 0;
+  for (;;) {
+    if (L >= cap && (i > 0 || j > 0)) {  // cannot happen with valid planes
+      res.status = TSQ_E_CUDA;
+      return;
+    }
+    if (state == 0) {
+      if (A.local) {
+        if (i == 0 || j == 0 || (pl.nib(i, j) & 3) == kDirStop) break;
+      } else if (i == 0 && j == 0) {
+        break;
+      }
+      if (i == 0) {  // global top row: one horizontal gap run
+        ++L;
+        out_a[cap - L] = '-';
+        out_b[cap - L] = char(b[j - 1]);
+        --j;
+        continue;
+      }
+      if (j == 0) {  // global left column: one vertical gap run
+        ++L;
+        out_a[cap - L] = char(a[i - 1]);
+        out_b[cap - L] = '-';
+        --i;
+        continue;
+      }
+      const int hd = pl.nib(i, j) & 3;
+      if (hd == kDirDiag) {
+        ++L;
+        out_a[cap - L] = char(a[i - 1]);
+        out_b[cap - L] = char(b[j - 1]);
+        ident += a[i - 1] == b[j - 1];
+        --i;
+        --j;
+      } else {
+        state = hd;
+      }
+    } else if (state == 1) {
+      // An E run always ends inside the matrix (E(i,0) is minus infinity);
+      // if the planes say otherwise, stop instead of leaving the matrix.
+      if (j <= 0 || i <= 0) {
+        res.status = TSQ_E_CUDA;
+        return;
+      }
+      const int d = pl.nib(i, j);
+      ++L;
+      out_a[cap - L] = '-';
+      out_b[cap - L] = char(b[j - 1]);
+      --j;
+      if (d & 4) state = 0;
+    } else {
+      if (i <= 0 || j <= 0) {
+        res.status = TSQ_E_CUDA;
+        return;
+      }
+      const int d = pl.nib(i, j);
+      ++L;
+      out_a[cap - L] = char(a[i - 1]);
+      out_b[cap - L] = '-';
+      --i;
+      if (d & 8) state = 0;
+    }
+  }
+  res.a_begin = i;
+  res.b_begin = j;
+  if (!A.local) {
+    res.a_end = m;
+    res.b_end = n;
+  }
+  res.n_cols = int32_t(L);
+  res.n_ident = ident;
+}
+
+__global__ void encode_kernel(const uint8_t *__restrict__ seqs, int64_t len, const uint8_t *__restrict__ lut,
+                              uint8_t *__restrict__ codes) {
+  __shared__ uint8_t s_lut[256];
+  s_lut[threadIdx.x] = lut[threadIdx.x];
+  __syncthreads();
+  // 16 residues per thread per iteration through 128-bit loads where the
+  // buffer allows it; the tail goes byte by byte.
+  const int64_t nvec = len / 16;
+  const uint4 *src = reinterpret_cast<const uint4 *>(seqs);
+  uint4 *dst = reinterpret_cast<uint4 *>(codes);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += stride) {
+    uint4 w = src[v];
+    uint32_t *x = reinterpret_cast<uint32_t *>(&w);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t u = x[q];
+      x[q] = uint32_t(s_lut[u & 0xFF]) | (uint32_t(s_lut[(u >> 8) & 0xFF]) << 8) |
+             (uint32_t(s_lut[(u >> 16) & 0xFF]) << 16) | (uint32_t(s_lut[u >> 24]) << 24);
+    }
+    dst[v] = w;
+  }
+  for (int64_t k = nvec * 16 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < len; k += stride)
+    codes[k] = s_lut[seqs[k]];
+}
+
+}  // namespace
+
+cudaError_t launch_walk(const WalkArgs &a, cudaStream_t st) {
+  if (a.n_tasks <= 0) return cudaSuccess;
+  const int threads = 128;
+  const int blocks = (a.n_tasks + threads - 1) / threads;
+  walk_kernel<<<blocks, threads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_encode(const uint8_t *seqs, int64_t len, const uint8_t *lut_dev, uint8_t *codes,
+                          cudaStream_t st) {
+  if (len <= 0) return cudaSuccess;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t work = (len + 15) / 16;
+  int blocks = int(std::min<int64_t>((work + 255) / 256, (int64_t)sms * 8));
+  if (blocks < 1) blocks = 1;
+  encode_kernel<<<blocks, 256, 0, st>>>(seqs, len, lut_dev, codes);
+  return cudaGetLastError();
+}
+
+}  // namespace tsq
