@@ -54,6 +54,8 @@ def parse_args():
     ap.add_argument("--plain-pairs", type=int, default=2000)
     ap.add_argument("--e2e-steps", type=int, default=0, help="0 = same as --steps")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile", type=int, default=0, metavar="PAIRS",
+                    help="profiling case: only the batched leg over the first PAIRS pairs, no graph")
     return ap.parse_args()
 
 
@@ -311,8 +313,32 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_profile(args):
+    """Small case for ncu: the device-resident batch over a prefix of the
+    workload, launched without a graph so each kernel is a separate launch."""
+    import torch
+
+    from tweakseq_gb300 import aligner as A
+    from tweakseq_gb300 import build as B
+    from tweakseq_gb300 import workloads as W
+
+    B.build()
+    ps = W.uneven_pairs()
+    sub = ps.subset(np.arange(min(args.profile, len(ps))))
+    batch = A.Batch(sub, output="score", use_graph=False)
+    for _ in range(args.warmup + args.steps):
+        batch.run()
+    torch.cuda.synchronize()
+    st = batch.stats()
+    print(json.dumps({"profile_pairs": len(sub), "cells": sub.cells, "fill_ms": st["fill_ms"],
+                      "gcups": sub.cells / (st["fill_ms"] * 1e-3) / 1e9, "launches_per_run": st["launches"]}))
+
+
 def main():
     args = parse_args()
+    if args.profile:
+        run_profile(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -312,13 +312,20 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
 
 namespace {
 
+// Inside stream capture an event record becomes an external event-record
+// node, so the event can still be timed after each graph launch.
+cudaError_t record(tsq_batch *b, int k) {
+  return b->capturing ? cudaEventRecordWithFlags(b->ev[k], b->stream, cudaEventRecordExternal)
+                      : cudaEventRecord(b->ev[k], b->stream);
+}
+
 int enqueue_run(tsq_batch *b) {
   cudaStream_t st = b->stream;
   const int nl = int(b->launches.size());
   TSQ_TRY(cudaMemsetAsync(b->counters.p, 0, sizeof(int32_t) * (size_t(nl) + 1), st));
-  TSQ_TRY(cudaEventRecord(b->ev[0], st));
+  TSQ_TRY(record(b, 0));
   TSQ_TRY(launch_encode(b->seqs.as<uint8_t>(), b->seqs_len, b->lut.as<uint8_t>(), b->codes.as<uint8_t>(), st));
-  TSQ_TRY(cudaEventRecord(b->ev[1], st));
+  TSQ_TRY(record(b, 1));
   for (int l = 0; l < nl; ++l) {
     const Launch &L = b->launches[size_t(l)];
     FillArgs a{};
@@ -339,7 +346,7 @@ int enqueue_run(tsq_batch *b) {
     a.overflow = nullptr;
     TSQ_TRY(launch_fill(L.sh, b->out_mode, b->local, a, L.blocks, st));
   }
-  TSQ_TRY(cudaEventRecord(b->ev[2], st));
+  TSQ_TRY(record(b, 2));
   if (b->out_mode == kOutTrace) {
     WalkArgs w{};
     w.seqs = b->seqs.as<uint8_t>();
@@ -357,7 +364,7 @@ int enqueue_run(tsq_batch *b) {
     w.aln_off = b->aln_off.as<int64_t>();
     TSQ_TRY(launch_walk(w, st));
   }
-  TSQ_TRY(cudaEventRecord(b->ev[3], st));
+  TSQ_TRY(record(b, 3));
   return TSQ_OK;
 }
 
@@ -372,7 +379,9 @@ int batch_run_async(tsq_batch *b) {
   } else {
     if (!b->gexec) {
       TSQ_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      b->capturing = true;
       const int rc = enqueue_run(b);
+      b->capturing = false;
       cudaGraph_t g = nullptr;
       const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
       if (rc) {
@@ -383,7 +392,9 @@ int batch_run_async(tsq_batch *b) {
       b->graph = g;
       TSQ_TRY(cudaGraphInstantiate(&b->gexec, b->graph, 0));
     }
+    TSQ_TRY(cudaEventRecord(b->ev[4], b->stream));
     TSQ_TRY(cudaGraphLaunch(b->gexec, b->stream));
+    TSQ_TRY(cudaEventRecord(b->ev[5], b->stream));
   }
   b->has_run = true;
   return TSQ_OK;
@@ -392,9 +403,19 @@ int batch_run_async(tsq_batch *b) {
 int batch_sync(tsq_batch *b) {
   if (!b) return TSQ_E_INVALID_ARG;
   TSQ_TRY(cudaStreamSynchronize(b->stream));
+  if (!b->has_run) return TSQ_OK;
   float total = 0.f, fill = 0.f;
-  if (b->has_run && cudaEventElapsedTime(&total, b->ev[0], b->ev[3]) == cudaSuccess) b->stats.device_ms = total;
-  if (b->has_run && cudaEventElapsedTime(&fill, b->ev[1], b->ev[2]) == cudaSuccess) b->stats.fill_ms = fill;
+  if (cudaEventElapsedTime(&total, b->ev[0], b->ev[3]) == cudaSuccess) {
+    b->stats.device_ms = total;
+  } else if (b->use_graph && cudaEventElapsedTime(&total, b->ev[4], b->ev[5]) == cudaSuccess) {
+    b->stats.device_ms = total;
+  }
+  if (cudaEventElapsedTime(&fill, b->ev[1], b->ev[2]) == cudaSuccess) {
+    b->stats.fill_ms = fill;
+  } else {
+    b->stats.fill_ms = b->stats.device_ms;  // whole graph when nodes cannot be timed
+  }
+  cudaGetLastError();  // a failed elapsed-time query is not a sticky error
   return TSQ_OK;
 }
 

@@ -71,7 +71,10 @@ bool tune_table_pick(int out_mode, int m, int n, Shape *sh);
 struct tsq_batch {
   int device = 0;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // ev[0..3]: run start, fill start, fill end, run end (inside the graph
+  // when captured); ev[4..5]: around a graph launch.
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  bool capturing = false;
   tsq::Scheme scheme{};
   tsq_params params{};
   int out_mode = tsq::kOutScore;
