@@ -83,25 +83,29 @@ constexpr int64_t kMaxLen = (1 << 20) - 1;
 }  // namespace
 
 Shape ShapeChooser::pick(int m, int n) const {
-  // Enough warps to fill every SM about 24 deep ...
+  // Lanes per pair G: (1) enough groups to fill every SM about 24 warps
+  // deep; (2) enough lanes that this pair's sweep -- about m*n / (G*R)
+  // dependent steps -- stays under half the balanced per-lane work of the
+  // batch, so a long pair does not become the tail; (3) no more lanes than
+  // its rows can use.
   const int64_t target_warps = int64_t(sms) * 24;
   int g_occ = npairs > 0 ? pow2ceil((target_warps * 32 + npairs - 1) / npairs) : 32;
-  g_occ = std::max(4, std::min(32, g_occ));
+  int g_lat = 1;
+  if (avg_lane_steps > 0) {
+    const double steps_at_g1 = double(m) * double(n) / kR;
+    g_lat = pow2ceil(int64_t(steps_at_g1 / (0.5 * avg_lane_steps)) + 1);
+  }
+  const int rows_cap = pow2ceil((m + kR - 1) / kR);
+  int G = std::max(g_occ, g_lat);
   Shape sh{};
   if (use_table && tune_table_pick(out_mode, m, n, &sh) && shape_supported(sh, out_mode, local)) {
-    if (!tune_forced() && sh.G < g_occ) {
-      Shape wider = sh;
-      wider.G = g_occ;
-      if (shape_supported(wider, out_mode, local)) sh = wider;
-    }
-    return sh;
+    if (tune_forced()) return sh;
+    G = std::max(G, sh.G);
+  } else {
+    sh.R = kR;
+    sh.i16 = 0;
   }
-  // ... and no more lanes per pair than its rows can use.
-  sh.R = kR;
-  sh.i16 = 0;
-  const int rows_cap = pow2ceil((m + kR - 1) / kR);
-  sh.G = std::max(4, std::min(g_occ, rows_cap));
-  (void)n;
+  sh.G = std::max(4, std::min(32, std::min(G, std::max(4, rows_cap))));
   return sh;
 }
 
@@ -196,6 +200,10 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   ch.local = b->local;
   ch.sms = sms;
   ch.npairs = plain ? 1 : n;
+  if (!plain) {
+    const double lanes = double(sms) * 24.0 * 32.0;
+    ch.avg_lane_steps = double(cells) / (lanes * kR);
+  }
   ch.use_table = b->autotune && tune_table_loaded();
   std::vector<int32_t> gsel(static_cast<size_t>(n));
   std::vector<int32_t> rsel(static_cast<size_t>(n));
@@ -220,36 +228,59 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
     if (nx != ny) return nx > ny;
     return x < y;
   });
-  b->launches.clear();
-  const int BW = b->out_mode == kOutIdent ? 4 : 2;
-  int64_t bnd_total = 0;
+  // Warp tasks: consecutive pairs of one bucket, 32/G per warp; their cost
+  // is the longest sweep among them (bands x steps).  Longest first.
+  std::vector<int2> wt;
+  std::vector<int64_t> wcost;
   for (int64_t s = 0; s < n;) {
+    const int32_t k0 = order[size_t(s)];
+    const int G = gsel[size_t(k0)];
+    const int per = 32 / G;
     int64_t e = s;
-    const int G = gsel[size_t(order[size_t(s)])], R = rsel[size_t(order[size_t(s)])];
-    int32_t cols = 1;
-    while (e < n && gsel[size_t(order[size_t(e)])] == G && rsel[size_t(order[size_t(e)])] == R) {
-      cols = std::max(cols, b->pairs_h[size_t(order[size_t(e)])].b_len + 1);
+    int64_t cost = 0;
+    while (e < n && e - s < per && gsel[size_t(order[size_t(e)])] == G) {
+      const int32_t k = order[size_t(e)];
+      cost = std::max<int64_t>(cost, int64_t(bands(k)) * (b->pairs_h[size_t(k)].b_len + G - 1));
       ++e;
     }
-    Launch L;
-    L.sh = Shape{G, R, 0};
-    L.task_begin = int32_t(s);
-    L.n_tasks = int32_t(e - s);
-    const int max_blocks = fill_blocks(L.sh, b->out_mode, b->local);
-    if (max_blocks <= 0) return TSQ_E_CUDA;
-    const int64_t needed = (int64_t(L.n_tasks) * G + fill_threads() - 1) / fill_threads();
-    L.blocks = int32_t(std::max<int64_t>(1, std::min<int64_t>(max_blocks, needed)));
-    L.slots = L.blocks * (fill_threads() / G);
-    L.bnd_cols = cols;
-    L.bnd_offset = bnd_total;
-    bnd_total += int64_t(L.slots) * BW * cols;
-    b->launches.push_back(L);
+    wt.push_back(make_int2(int32_t(s), (G << 16) | int32_t(e - s)));
+    wcost.push_back(cost);
     s = e;
+  }
+  std::vector<int32_t> worder(wt.size());
+  std::iota(worder.begin(), worder.end(), 0);
+  std::stable_sort(worder.begin(), worder.end(), [&](int32_t x, int32_t y) { return wcost[size_t(x)] > wcost[size_t(y)]; });
+  std::vector<int2> wt_sorted(wt.size());
+  for (size_t k = 0; k < wt.size(); ++k) wt_sorted[k] = wt[size_t(worder[k])];
+
+  b->launches.clear();
+  int64_t bnd_total = 0;
+  if (!wt_sorted.empty()) {
+    Launch L;
+    L.R = kR;
+    L.i16 = 0;
+    L.wt_begin = 0;
+    L.n_wtasks = int32_t(wt_sorted.size());
+    const int max_blocks = fill_blocks(L.R, L.i16, b->out_mode, b->local);
+    if (max_blocks <= 0) return TSQ_E_CUDA;
+    const int warps_per_block = fill_threads() / 32;
+    const int64_t needed = (int64_t(L.n_wtasks) + warps_per_block - 1) / warps_per_block;
+    L.blocks = int32_t(std::max<int64_t>(1, std::min<int64_t>(max_blocks, needed)));
+    // Whole staged chunks are copied, so rows are padded to a chunk past n.
+    L.bnd_cols = ((max_n + 31) / 32 + 1) * 32;
+    L.bnd_offset = 0;
+    bnd_total = int64_t(L.blocks) * warps_per_block * 8 * L.bnd_cols *
+                int64_t(fill_bnd_entry_bytes(L.i16, b->out_mode));
+    b->launches.push_back(L);
   }
   b->stats.pairs = n;
   b->stats.cells = cells;
   b->stats.launches = int32_t(b->launches.size()) + 1 + (b->out_mode == kOutTrace ? 1 : 0);
-  b->stats.buckets = int32_t(b->launches.size());
+  {
+    std::vector<int32_t> gs(gsel);
+    std::sort(gs.begin(), gs.end());
+    b->stats.buckets = int32_t(std::unique(gs.begin(), gs.end()) - gs.begin());
+  }
 
   // ---- traceback layout ----------------------------------------------------
   std::vector<int64_t> ploff;
@@ -271,12 +302,14 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   // ---- device buffers and uploads -------------------------------------------
   uint8_t lut[256];
   build_lut(sc, lut);
-  TSQ_TRY(b->seqs.ensure(size_t(seqs_len) + 16));
-  TSQ_TRY(b->codes.ensure(size_t(seqs_len) + 16));
+  // Staged code chunks read up to 64 bytes past a sequence.
+  TSQ_TRY(b->seqs.ensure(size_t(seqs_len) + 128));
+  TSQ_TRY(b->codes.ensure(size_t(seqs_len) + 128));
   TSQ_TRY(b->pairs.ensure(sizeof(PairDev) * size_t(n)));
   TSQ_TRY(b->tasks.ensure(sizeof(int32_t) * size_t(n)));
   TSQ_TRY(b->res.ensure(sizeof(ResultDev) * size_t(n)));
-  TSQ_TRY(b->bnd.ensure(sizeof(int32_t) * size_t(bnd_total)));
+  TSQ_TRY(b->bnd.ensure(size_t(bnd_total)));
+  TSQ_TRY(b->wtasks.ensure(sizeof(int2) * std::max<size_t>(1, wt_sorted.size())));
   TSQ_TRY(b->counters.ensure(sizeof(int32_t) * (b->launches.size() + 1)));
   TSQ_TRY(b->lut.ensure(256));
   TSQ_TRY(b->matrix.ensure(kLetters * kLetters));
@@ -295,6 +328,8 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   if (n > 0) {
     TSQ_TRY(cudaMemcpyAsync(b->pairs.p, b->pairs_h.data(), sizeof(PairDev) * size_t(n), cudaMemcpyHostToDevice, st));
     TSQ_TRY(cudaMemcpyAsync(b->tasks.p, order.data(), sizeof(int32_t) * size_t(n), cudaMemcpyHostToDevice, st));
+    TSQ_TRY(cudaMemcpyAsync(b->wtasks.p, wt_sorted.data(), sizeof(int2) * wt_sorted.size(), cudaMemcpyHostToDevice,
+                            st));
   }
   TSQ_TRY(cudaMemcpyAsync(b->lut.p, lut, 256, cudaMemcpyHostToDevice, st));
   TSQ_TRY(cudaMemcpyAsync(b->matrix.p, sc.score, kLetters * kLetters, cudaMemcpyHostToDevice, st));
@@ -331,20 +366,20 @@ int enqueue_run(tsq_batch *b) {
     FillArgs a{};
     a.codes = b->codes.as<uint8_t>();
     a.pairs = b->pairs.as<PairDev>();
-    a.tasks = b->tasks.as<int32_t>() + L.task_begin;
-    a.n_tasks = L.n_tasks;
+    a.tasks = b->tasks.as<int32_t>();
+    a.wtasks = b->wtasks.as<int2>() + L.wt_begin;
+    a.n_wtasks = L.n_wtasks;
     a.counter = b->counters.as<int32_t>() + l;
     a.matrix = b->matrix.as<int8_t>();
     a.gap_open = b->params.gap_open;
     a.gap_extend = b->params.gap_extend;
     a.res = b->res.as<ResultDev>();
-    a.bnd = b->bnd.as<int32_t>() + L.bnd_offset;
+    a.bnd = reinterpret_cast<int32_t *>(b->bnd.as<uint8_t>() + L.bnd_offset);
     a.bnd_cols = L.bnd_cols;
-    a.n_slots = L.slots;
     a.planes = b->planes.as<uint8_t>();
     a.plane_off = b->plane_off.as<int64_t>();
     a.overflow = nullptr;
-    TSQ_TRY(launch_fill(L.sh, b->out_mode, b->local, a, L.blocks, st));
+    TSQ_TRY(launch_fill(L.R, L.i16, b->out_mode, b->local, a, L.blocks, st));
   }
   TSQ_TRY(record(b, 2));
   if (b->out_mode == kOutTrace) {

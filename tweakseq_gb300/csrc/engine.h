@@ -41,14 +41,14 @@ struct PinBuf {
   PinBuf &operator=(const PinBuf &) = delete;
 };
 
-// One persistent fill launch over a bucket of pairs of one kernel shape.
+// One persistent fill launch: every warp task of one row height R and lane
+// type, all lane widths G mixed, longest first.
 struct Launch {
-  Shape sh;
-  int32_t task_begin = 0, n_tasks = 0;
+  int R = 8, i16 = 0;
+  int32_t wt_begin = 0, n_wtasks = 0;  // slice of the warp-task list
   int32_t blocks = 0;
   int32_t bnd_cols = 0;
-  int64_t bnd_offset = 0;  // int32 elements into the boundary scratch
-  int32_t slots = 0;
+  int64_t bnd_offset = 0;  // bytes into the boundary scratch
 };
 
 // Kernel-shape choice.  A tuned table (lengths -> shape) overrides the
@@ -58,6 +58,9 @@ struct ShapeChooser {
   bool local = false;
   int sms = 152;
   int64_t npairs = 0;
+  // Balanced steps per resident lane over the whole batch: no pair may need
+  // more than about half of it, or it becomes the batch's tail.
+  double avg_lane_steps = 0.0;
   bool use_table = false;
   Shape pick(int m, int n) const;
 };
@@ -90,7 +93,7 @@ struct tsq_batch {
   int64_t aln_bytes = 0;
   bool has_run = false;
 
-  tsq::DevBuf seqs, codes, pairs, tasks, res, bnd, planes, plane_off, aln, aln_off, shape_g, shape_r, counters,
+  tsq::DevBuf seqs, codes, pairs, tasks, wtasks, res, bnd, planes, plane_off, aln, aln_off, shape_g, shape_r, counters,
       lut, matrix;
   tsq::PinBuf res_h, aln_h;
 

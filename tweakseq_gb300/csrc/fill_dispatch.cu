@@ -1,54 +1,58 @@
-// fill_dispatch.cu -- picks the fill kernel instantiation for a shape.
+// fill_dispatch.cu -- picks the fill kernel for an output mode and lane type.
 #include "fill_i32.cuh"
 
 namespace tsq {
 namespace fill {
 template <int OUT>
-cudaError_t launch_i32(const Shape &sh, bool local, const FillArgs &a, int blocks, size_t smem, cudaStream_t st);
+cudaError_t launch_i32(bool local, const FillArgs &a, int blocks, size_t smem, cudaStream_t st);
 template <int OUT>
-int occupancy_i32(const Shape &sh, bool local, size_t smem);
-template <int OUT>
-bool has_i32(const Shape &sh);
+int occupancy_i32(bool local, size_t smem);
 }  // namespace fill
 
 int fill_threads() { return fill::kThreads; }
 
-size_t fill_smem_bytes(const Shape &sh) {
-  return size_t(fill::kMatBytes) + size_t(kLetters) * fill::kThreads * sh.R;
+size_t fill_smem_bytes(int R, int i16, int out_mode) {
+  (void)i16;
+  const size_t top = out_mode == kOutIdent ? 16 : 8;
+  return size_t(fill::kMatBytes) + size_t(kLetters) * fill::kThreads * size_t(R) +
+         size_t(fill::kSlotsPerBlock) * (fill::kTopRing * top + fill::kCodeRing);
+}
+
+size_t fill_bnd_entry_bytes(int i16, int out_mode) {
+  (void)i16;
+  return out_mode == kOutIdent ? 16 : 8;
 }
 
 bool shape_supported(const Shape &sh, int out_mode, bool local) {
   (void)local;
-  if (sh.i16) return false;
-  switch (out_mode) {
-    case kOutScore: return fill::has_i32<kOutScore>(sh);
-    case kOutIdent: return fill::has_i32<kOutIdent>(sh);
-    case kOutTrace: return fill::has_i32<kOutTrace>(sh);
-  }
-  return false;
+  (void)out_mode;
+  if (sh.i16 || sh.R != 8) return false;
+  return sh.G == 4 || sh.G == 8 || sh.G == 16 || sh.G == 32;
 }
 
-int fill_blocks(const Shape &sh, int out_mode, bool local) {
+int fill_blocks(int R, int i16, int out_mode, bool local) {
+  if (R != 8 || i16) return 0;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t smem = fill_smem_bytes(sh);
+  const size_t smem = fill_smem_bytes(R, i16, out_mode);
   int per_sm = 0;
   switch (out_mode) {
-    case kOutScore: per_sm = fill::occupancy_i32<kOutScore>(sh, local, smem); break;
-    case kOutIdent: per_sm = fill::occupancy_i32<kOutIdent>(sh, local, smem); break;
-    case kOutTrace: per_sm = fill::occupancy_i32<kOutTrace>(sh, local, smem); break;
+    case kOutScore: per_sm = fill::occupancy_i32<kOutScore>(local, smem); break;
+    case kOutIdent: per_sm = fill::occupancy_i32<kOutIdent>(local, smem); break;
+    case kOutTrace: per_sm = fill::occupancy_i32<kOutTrace>(local, smem); break;
   }
   return per_sm * sms;
 }
 
-cudaError_t launch_fill(const Shape &sh, int out_mode, bool local, const FillArgs &a, int blocks,
+cudaError_t launch_fill(int R, int i16, int out_mode, bool local, const FillArgs &a, int blocks,
                         cudaStream_t st) {
-  const size_t smem = fill_smem_bytes(sh);
+  if (R != 8 || i16) return cudaErrorInvalidValue;
+  const size_t smem = fill_smem_bytes(R, i16, out_mode);
   switch (out_mode) {
-    case kOutScore: return fill::launch_i32<kOutScore>(sh, local, a, blocks, smem, st);
-    case kOutIdent: return fill::launch_i32<kOutIdent>(sh, local, a, blocks, smem, st);
-    case kOutTrace: return fill::launch_i32<kOutTrace>(sh, local, a, blocks, smem, st);
+    case kOutScore: return fill::launch_i32<kOutScore>(local, a, blocks, smem, st);
+    case kOutIdent: return fill::launch_i32<kOutIdent>(local, a, blocks, smem, st);
+    case kOutTrace: return fill::launch_i32<kOutTrace>(local, a, blocks, smem, st);
   }
   return cudaErrorInvalidValue;
 }

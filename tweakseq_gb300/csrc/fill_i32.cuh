@@ -13,7 +13,14 @@
 // the group works on the anti-diagonal s of the band: lane t computes column
 // s - t.  The bottom row of lane t (H and F) reaches lane t+1 by a warp
 // shuffle; the bottom row of the band (lane G-1) goes to a scratch row in
-// HBM and is the top row of the next band, read back by lane 0.
+// HBM and is the top row of the next band, read back by lane 0.  Row 0 of
+// the matrix is written into that scratch row before the first band, so
+// every band reads its top row the same way.
+//
+// Latency hiding.  The top row and b's residue codes are staged per group in
+// shared-memory rings by cp.async one 32-column chunk ahead; each step reads
+// the next step's code, profile word and (lane 0) top entry from shared
+// memory, so no global load sits on the step's dependency chain.
 //
 // Scores come from a per-lane query profile in shared memory: for each of
 // the 26 letters, the R int8 scores of the lane's rows, laid out
@@ -35,6 +42,7 @@ namespace fill {
 
 constexpr int kThreads = 256;   // 8 warps per block
 constexpr int kMatBytes = 704;  // 26*26 int8 rounded up to a 64-byte multiple
+constexpr int kAhead = 4;       // step-loop unroll
 
 // Sign-extends byte K of w to 32 bits with one PRMT (selector bit 3 of each
 // nibble replicates the sign of the chosen byte).
@@ -45,18 +53,14 @@ __device__ __forceinline__ int32_t sbyte(uint32_t w) {
   return int32_t(d);
 }
 
-template <int R>
-struct ProfWord;
-template <>
-struct ProfWord<4> {
-  using T = uint32_t;
-  __device__ static uint32_t word(T v, int k) { return v; }
-};
-template <>
-struct ProfWord<8> {
-  using T = uint2;
-  __device__ static uint32_t word(T v, int k) { return k == 0 ? v.x : v.y; }
-};
+__device__ __forceinline__ int32_t sbyte_dyn(uint32_t w, int k) {
+  switch (k & 3) {
+    case 0: return sbyte<0>(w);
+    case 1: return sbyte<1>(w);
+    case 2: return sbyte<2>(w);
+    default: return sbyte<3>(w);
+  }
+}
 
 // Global-mode boundary value H(i,0) = H(0,i) = -(open + i*ext), H(0,0) = 0.
 __device__ __forceinline__ int32_t edge_h(int i, int32_t go, int32_t ge, bool local) {
@@ -81,52 +85,104 @@ __device__ __forceinline__ T group_max(T v) {
   return v;
 }
 
+// Top-row entry carried from band to band: H and F, plus the path counts of
+// both in identity mode.
+template <int OUT>
+struct TopT {
+  using T = int2;
+};
+template <>
+struct TopT<kOutIdent> {
+  using T = int4;
+};
+
+// ---- staging rings --------------------------------------------------------
+// Each group keeps, in shared memory, a 64-column ring of its top row and a
+// 128-byte ring of b's residue codes.  They are filled by cp.async 32
+// columns ahead of use (one chunk in flight while the group sweeps the
+// previous one), so the step loop reads only shared memory.
+constexpr int kChunk = 32;       // columns per staged chunk
+constexpr int kTopRing = 64;     // top-row ring entries per group
+constexpr int kCodeRing = 128;   // code ring bytes per group
+constexpr int kSlotsPerBlock = kThreads / 32 * 8;  // 8 group slots per warp
+
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Issues the copies of chunk k (columns [32k, 32k+32) of the top row and the
+// code bytes of columns [32k, 32k+32]) for one group; lane t of the group
+// takes copies t, t+G, ...  Nothing is copied past the pair's columns.
+template <int G, typename Top>
+__device__ __forceinline__ void stage_chunk(int k, int t, int nact, const Top *top_g, Top *top_ring,
+                                            const uint8_t *codes, int64_t boff, uint8_t *code_ring) {
+  constexpr int kPer = 16 / int(sizeof(Top));                  // entries per 16-byte copy
+  constexpr int kTopCopies = kChunk / kPer;
+  constexpr int kCopies = kTopCopies + 3;
+  const int c0 = kChunk * k;
+  if (c0 >= nact) return;
+  const int64_t a0 = (boff + c0) & ~int64_t(15);
+#pragma unroll
+  for (int q0 = 0; q0 < kCopies; q0 += G) {
+    const int q = q0 + t;
+    if (q < kTopCopies) {
+      const int e = c0 + q * kPer;
+      cp_async16(top_ring + (e & (kTopRing - 1)), top_g + e);
+    } else if (q < kCopies) {
+      const int64_t a = a0 + 16 * (q - kTopCopies);
+      cp_async16(code_ring + (a & (kCodeRing - 1)), codes + a);
+    }
+  }
+}
+
+// One warp task: the warp's 32/G groups each take one pair (or idle).
 template <int G, int R, bool LOCAL, int OUT>
-__global__ void __launch_bounds__(kThreads) fill_i32_kernel(const FillArgs A) {
-  extern __shared__ __align__(16) uint8_t smem[];
-  int8_t *s_mat = reinterpret_cast<int8_t *>(smem);
-  uint8_t *s_prof = smem + kMatBytes;
-  using PW = ProfWord<R>;
-  using PT = typename PW::T;
-
-  for (int k = threadIdx.x; k < kLetters * kLetters; k += blockDim.x) s_mat[k] = A.matrix[k];
-  __syncthreads();
-
+__device__ __forceinline__ void fill_warp_task(const FillArgs &A, const int8_t *s_mat, uint2 *s_prof,
+                                               uint8_t *s_rings, int begin, int count, int warp_id) {
+  static_assert(R == 8, "the profile word layout assumes 8 rows per lane");
+  using Top = typename TopT<OUT>::T;
   constexpr int GPW = 32 / G;  // groups per warp
   constexpr int P = G * R;     // rows per band
   const int lane = threadIdx.x & 31;
   const int t = lane % G;
   const int gw = lane / G;
   const int32_t go = A.gap_open, ge = A.gap_extend, oe = go + ge;
-  const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int slot = warp_id * GPW + gw;
-  // Boundary scratch: one row of (H, F[, cH, cF]) per group.  Lane 0 of
-  // band k+1 reads column j before lane G-1 of the same band overwrites it:
-  // lane G-1's value for column j is computed from data lane 0 derived from
-  // that read, G-1 shuffles later, so one row suffices.
-  constexpr int BW = OUT == kOutIdent ? 4 : 2;
-  int32_t *bnd = A.bnd + (int64_t)slot * BW * A.bnd_cols;
-  PT *prof = reinterpret_cast<PT *>(s_prof) + threadIdx.x;  // + c * kThreads
+  // One top row per group.  Lane 0 of a band reads column j several steps
+  // before lane G-1 of the same band overwrites it, and lane G-1's value is
+  // computed from data derived from that read, so one row suffices.
+  Top *top = reinterpret_cast<Top *>(A.bnd) + ((int64_t)warp_id * 8 + gw) * A.bnd_cols;
+  const uint2 *prof = s_prof + threadIdx.x;  // + c * kThreads
+  (void)GPW;
+  // This group's staging rings.
+  const int gslot = (threadIdx.x >> 5) * 8 + gw;
+  Top *top_ring = reinterpret_cast<Top *>(s_rings) + gslot * kTopRing;
+  uint8_t *code_ring = s_rings + kSlotsPerBlock * kTopRing * sizeof(Top) + gslot * kCodeRing;
 
-  for (;;) {
-    int base_task = 0;
-    if (lane == 0) base_task = atomicAdd(A.counter, GPW);
-    base_task = __shfl_sync(0xffffffffu, base_task, 0);
-    if (base_task >= A.n_tasks) break;
-    const int task = base_task + gw;
-    const bool have = task < A.n_tasks;
-    const int pid = have ? A.tasks[task] : 0;
-    PairDev pr;
+  {
+    const bool have = gw < count;
+    const int pid = have ? A.tasks[begin + gw] : 0;
+    int m = 0, n = 0;
+    const uint8_t *qa_codes = A.codes, *qb_codes = A.codes;
+    int64_t boff = 0;
     if (have) {
-      pr = A.pairs[pid];
-    } else {
-      pr.a_off = pr.b_off = 0;
-      pr.a_len = pr.b_len = 0;
+      const PairDev pr = A.pairs[pid];
+      m = pr.a_len;
+      n = pr.b_len;
+      qa_codes = A.codes + pr.a_off;
+      qb_codes = A.codes + pr.b_off;
+      boff = pr.b_off;
     }
-    const int m = pr.a_len, n = pr.b_len;
-    const uint8_t *qa_codes = A.codes + pr.a_off;
-    const uint8_t *qb_codes = A.codes + pr.b_off;
-    const bool trivial = (m == 0 || n == 0);
+    // Residues are validated once per pair; a pair with an invalid residue
+    // is reported and not filled.
+    bool bad = false;
+    for (int k = t; k < m; k += G) bad |= qa_codes[k] >= kLetters;
+    for (int k = t; k < n; k += G) bad |= qb_codes[k] >= kLetters;
+    const unsigned gm = group_mask<G>(lane);
+    const bool gbad = (__ballot_sync(0xffffffffu, bad) & gm) != 0;
+    const bool trivial = (m == 0 || n == 0 || gbad);
     const int passes = trivial ? 0 : (m + P - 1) / P;
     const int steps = trivial ? 0 : n + G - 1;
     int max_passes = passes, max_steps = steps;
@@ -138,12 +194,21 @@ __global__ void __launch_bounds__(kThreads) fill_i32_kernel(const FillArgs A) {
     uint8_t *planes = nullptr;
     if constexpr (OUT == kOutTrace) planes = A.planes + (have ? A.plane_off[pid] : 0);
 
-    bool bad = false;
-    if (have && trivial) {
-      // No DP cells, but every residue is still validated.
-      for (int k = t; k < m; k += G) bad |= qa_codes[k] == kBadCode;
-      for (int k = t; k < n; k += G) bad |= qb_codes[k] == kBadCode;
+    // Row 0 of the matrix becomes the first top row.
+    if (!trivial) {
+      for (int j = t; j < n; j += G) {
+        Top v;
+        v.x = edge_h(j + 1, go, ge, LOCAL);
+        v.y = kNegInf;
+        if constexpr (OUT == kOutIdent) {
+          v.z = LOCAL ? 0 : j + 1;
+          v.w = 0;
+        }
+        top[j] = v;
+      }
     }
+    __syncwarp();
+
     // Local: best cell so far of this lane (value, 1-based row, 1-based col).
     int32_t lbest = 0, lrow = 0, lcol = 0;
     uint32_t lcnt = 0;
@@ -152,21 +217,21 @@ __global__ void __launch_bounds__(kThreads) fill_i32_kernel(const FillArgs A) {
 
     for (int pass = 0; pass < max_passes; ++pass) {
       const bool gact = pass < passes;
+      const int nact = gact ? n : 0;
       const int row0 = pass * P + t * R;  // rows row0+1 .. row0+R (1-based)
-      // Query codes and the lane's profile for this band.
+      // Query codes and the lane's profile for this band (padding rows: 0).
       int qa[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int i = row0 + r;
-        int c = (gact && i < m) ? qa_codes[i] : 0;
-        if (gact && i < m && c == kBadCode) bad = true;
-        qa[r] = (gact && i < m && c != kBadCode) ? c : -1;
+        qa[r] = (gact && i < m) ? int(qa_codes[i]) : -1;
       }
+      __syncwarp();
 #pragma unroll 2
       for (int c = 0; c < kLetters; ++c) {
-        uint32_t w[R / 4];
+        uint32_t w[2];
 #pragma unroll
-        for (int q = 0; q < R / 4; ++q) {
+        for (int q = 0; q < 2; ++q) {
           uint32_t v = 0;
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
@@ -176,10 +241,7 @@ __global__ void __launch_bounds__(kThreads) fill_i32_kernel(const FillArgs A) {
           }
           w[q] = v;
         }
-        if constexpr (R == 8)
-          prof[c * kThreads] = make_uint2(w[0], w[1]);
-        else
-          prof[c * kThreads] = w[0];
+        s_prof[c * kThreads + threadIdx.x] = make_uint2(w[0], w[1]);
       }
 
       int32_t H[R], E[R];
@@ -200,145 +262,159 @@ __global__ void __launch_bounds__(kThreads) fill_i32_kernel(const FillArgs A) {
       uint32_t cdiag = LOCAL ? 0u : uint32_t(row0);
       int32_t outH = 0, outF = kNegInf;
       uint32_t outCH = 0, outCF = 0;
-      int bc_next = 0;
-      {
-        const int jj = -t;
-        if (gact && jj >= 0 && jj < n) bc_next = qb_codes[jj];
-      }
 
-      for (int s = 0; s < max_steps; ++s) {
-        int32_t upH = __shfl_up_sync(0xffffffffu, outH, 1, G);
-        int32_t upF = __shfl_up_sync(0xffffffffu, outF, 1, G);
-        uint32_t upCH = 0, upCF = 0;
-        if constexpr (OUT == kOutIdent) {
-          upCH = __shfl_up_sync(0xffffffffu, outCH, 1, G);
-          upCF = __shfl_up_sync(0xffffffffu, outCF, 1, G);
-        }
-        const int jj = s - t;
-        const bool valid = gact && jj >= 0 && jj < n;
-        int bc = bc_next;
-        if (gact && jj + 1 >= 0 && jj + 1 < n) bc_next = qb_codes[jj + 1];
-        if (valid) {
-          if (bc == kBadCode) {
-            bad = true;
-            bc = 0;
-          }
-          if (t == 0) {
-            if (pass == 0) {
-              upH = edge_h(jj + 1, go, ge, LOCAL);
-              upF = kNegInf;
-              upCH = LOCAL ? 0u : uint32_t(jj + 1);
-              upCF = 0u;
-            } else {
-              upH = bnd[(jj + 1) * BW + 0];
-              upF = bnd[(jj + 1) * BW + 1];
-              if constexpr (OUT == kOutIdent) {
-                upCH = uint32_t(bnd[(jj + 1) * BW + 2]);
-                upCF = uint32_t(bnd[(jj + 1) * BW + 3]);
-              }
-            }
-          }
-          const PT pw = prof[bc * kThreads];
-          int32_t hu = upH, fv = upF, d = hdiag;
-          uint32_t chu = upCH, cfv = upCF, cd = cdiag;
-          hdiag = upH;
-          cdiag = upCH;
-          uint32_t tw = 0;
+      // Stage chunk 0 (and wait for it), then put chunk 1 in flight.
+      cp_async_wait_all();
+      __syncwarp();
+      stage_chunk<G>(0, t, nact, top, top_ring, A.codes, boff, code_ring);
+      cp_async_commit();
+      cp_async_wait_all();
+      __syncwarp();
+      stage_chunk<G>(1, t, nact, top, top_ring, A.codes, boff, code_ring);
+      cp_async_commit();
+
+      // Double-buffered per-step operands: slot (s & 1) holds what step s
+      // uses; step s loads slot ((s + 1) & 1) from the rings.
+      int cb[2];
+      uint2 pw[2];
+      Top tv[2];
+      cb[0] = min(int(code_ring[(boff - t) & (kCodeRing - 1)]), kLetters - 1);
+      pw[0] = prof[cb[0] * kThreads];
+      tv[0] = top_ring[0];
+
+      for (int s0 = 0; s0 < max_steps; s0 += kAhead) {
 #pragma unroll
-          for (int r = 0; r < R; ++r) {
-            const uint32_t wq = PW::word(pw, r / 4);
-            int32_t sc;
-            switch (r & 3) {
-              case 0: sc = sbyte<0>(wq); break;
-              case 1: sc = sbyte<1>(wq); break;
-              case 2: sc = sbyte<2>(wq); break;
-              default: sc = sbyte<3>(wq); break;
+        for (int k = 0; k < kAhead; ++k) {
+          const int s = s0 + k;
+          if (s < max_steps) {
+            if (((s + 1) & (kChunk - 1)) == 0) {
+              // Last step of a chunk: the next chunk (issued 32 steps ago)
+              // must have landed before this step reads its first column.
+              cp_async_wait_all();
+              __syncwarp();
+              stage_chunk<G>((s + 1) / kChunk + 1, t, nact, top, top_ring, A.codes, boff, code_ring);
+              cp_async_commit();
             }
-            const int32_t eo = H[r] - oe, ee = E[r] - ge;
-            const int32_t fo = hu - oe, fe = fv - ge;
-            const int32_t e = max(eo, ee);
-            const int32_t f = max(fo, fe);
-            const int32_t dd = d + sc;
-            int32_t h;
-            if constexpr (OUT == kOutScore) {
-              h = LOCAL ? __vimax3_s32_relu(dd, e, f) : __vimax3_s32(dd, e, f);
-              if constexpr (LOCAL) {
-                if (h > best[r]) {
-                  best[r] = h;
-                  bcol[r] = jj + 1;
-                }
-              }
-            } else {
-              const bool eopen = eo >= ee, fopen = fo >= fe;
-              int dir = kDirDiag;
-              h = dd;
-              if (e > h) {
-                h = e;
-                dir = kDirE;
-              }
-              if (f > h) {
-                h = f;
-                dir = kDirF;
-              }
-              if (LOCAL && h <= 0) {
-                h = 0;
-                dir = kDirStop;
-              }
-              if constexpr (OUT == kOutIdent) {
-                const uint32_t ce = (eopen ? cH[r] : cE[r]) + kCol;
-                const uint32_t cf = (fopen ? chu : cfv) + kCol;
-                const uint32_t cdd = cd + (qa[r] == bc ? kIdentCol : kCol);
-                uint32_t ch = dir == kDirDiag ? cdd : (dir == kDirE ? ce : cf);
-                if (LOCAL && dir == kDirStop) ch = 0u;
-                cd = cH[r];
-                cH[r] = ch;
-                cE[r] = ce;
-                chu = ch;
-                cfv = cf;
-                if constexpr (LOCAL) {
-                  if (h > best[r]) {
-                    best[r] = h;
-                    bcol[r] = jj + 1;
-                    bcnt[r] = ch;
-                  }
-                }
-              } else {
-                tw |= uint32_t(dir | (eopen ? 4 : 0) | (fopen ? 8 : 0)) << (4 * r);
-                if constexpr (LOCAL) {
-                  if (h > best[r]) {
-                    best[r] = h;
-                    bcol[r] = jj + 1;
-                  }
-                }
-              }
-            }
-            d = H[r];
-            H[r] = h;
-            E[r] = e;
-            hu = h;
-            fv = f;
-          }
-          outH = hu;
-          outF = fv;
-          outCH = chu;
-          outCF = cfv;
-          if (t == G - 1) {
-            bnd[(jj + 1) * BW + 0] = outH;
-            bnd[(jj + 1) * BW + 1] = outF;
+            int32_t upH = __shfl_up_sync(0xffffffffu, outH, 1, G);
+            int32_t upF = __shfl_up_sync(0xffffffffu, outF, 1, G);
+            uint32_t upCH = 0, upCF = 0;
             if constexpr (OUT == kOutIdent) {
-              bnd[(jj + 1) * BW + 2] = int32_t(outCH);
-              bnd[(jj + 1) * BW + 3] = int32_t(outCF);
+              upCH = __shfl_up_sync(0xffffffffu, outCH, 1, G);
+              upCF = __shfl_up_sync(0xffffffffu, outCF, 1, G);
             }
-          }
-          if constexpr (OUT == kOutTrace) {
-            const int64_t entry = ((int64_t)pass * (n + G - 1) + s) * G + t;
-            if constexpr (R == 8)
-              reinterpret_cast<uint32_t *>(planes)[entry] = tw;
-            else
-              reinterpret_cast<uint16_t *>(planes)[entry] = uint16_t(tw);
+            const int jj = s - t;
+            const bool valid = (unsigned)jj < (unsigned)nact;
+            const int bc = cb[k & 1];
+            const uint2 pcur = pw[k & 1];
+            // Operands of the next step.  Codes outside the pair are clamped
+            // into the table; those steps are masked anyway.
+            cb[(k + 1) & 1] = min(int(code_ring[(boff + jj + 1) & (kCodeRing - 1)]), kLetters - 1);
+            pw[(k + 1) & 1] = prof[cb[(k + 1) & 1] * kThreads];
+            if (t == 0) {
+              upH = tv[k & 1].x;
+              upF = tv[k & 1].y;
+              if constexpr (OUT == kOutIdent) {
+                upCH = uint32_t(tv[k & 1].z);
+                upCF = uint32_t(tv[k & 1].w);
+              }
+              tv[(k + 1) & 1] = top_ring[(jj + 1) & (kTopRing - 1)];
+            }
+            if (valid) {
+              int32_t hu = upH, fv = upF, d = hdiag;
+              uint32_t chu = upCH, cfv = upCF, cd = cdiag;
+              hdiag = upH;
+              cdiag = upCH;
+              uint32_t tw = 0;
+#pragma unroll
+              for (int r = 0; r < R; ++r) {
+                const int32_t sc = sbyte_dyn(r < 4 ? pcur.x : pcur.y, r);
+                const int32_t eo = H[r] - oe, ee = E[r] - ge;
+                const int32_t fo = hu - oe, fe = fv - ge;
+                const int32_t e = max(eo, ee);
+                const int32_t f = max(fo, fe);
+                const int32_t dd = d + sc;
+                int32_t h;
+                if constexpr (OUT == kOutScore) {
+                  h = LOCAL ? __vimax3_s32_relu(dd, e, f) : __vimax3_s32(dd, e, f);
+                  if constexpr (LOCAL) {
+                    if (h > best[r]) {
+                      best[r] = h;
+                      bcol[r] = jj + 1;
+                    }
+                  }
+                } else {
+                  const bool eopen = eo >= ee, fopen = fo >= fe;
+                  int dir = kDirDiag;
+                  h = dd;
+                  if (e > h) {
+                    h = e;
+                    dir = kDirE;
+                  }
+                  if (f > h) {
+                    h = f;
+                    dir = kDirF;
+                  }
+                  if (LOCAL && h <= 0) {
+                    h = 0;
+                    dir = kDirStop;
+                  }
+                  if constexpr (OUT == kOutIdent) {
+                    const uint32_t ce = (eopen ? cH[r] : cE[r]) + kCol;
+                    const uint32_t cfn = (fopen ? chu : cfv) + kCol;
+                    const uint32_t cdd = cd + (qa[r] == bc ? kIdentCol : kCol);
+                    uint32_t ch = dir == kDirDiag ? cdd : (dir == kDirE ? ce : cfn);
+                    if (LOCAL && dir == kDirStop) ch = 0u;
+                    cd = cH[r];
+                    cH[r] = ch;
+                    cE[r] = ce;
+                    chu = ch;
+                    cfv = cfn;
+                    if constexpr (LOCAL) {
+                      if (h > best[r]) {
+                        best[r] = h;
+                        bcol[r] = jj + 1;
+                        bcnt[r] = ch;
+                      }
+                    }
+                  } else {
+                    tw |= uint32_t(dir | (eopen ? 4 : 0) | (fopen ? 8 : 0)) << (4 * r);
+                    if constexpr (LOCAL) {
+                      if (h > best[r]) {
+                        best[r] = h;
+                        bcol[r] = jj + 1;
+                      }
+                    }
+                  }
+                }
+                d = H[r];
+                H[r] = h;
+                E[r] = e;
+                hu = h;
+                fv = f;
+              }
+              outH = hu;
+              outF = fv;
+              outCH = chu;
+              outCF = cfv;
+              if (t == G - 1) {
+                Top v;
+                v.x = outH;
+                v.y = outF;
+                if constexpr (OUT == kOutIdent) {
+                  v.z = int32_t(outCH);
+                  v.w = int32_t(outCF);
+                }
+                top[jj] = v;
+              }
+              if constexpr (OUT == kOutTrace) {
+                const int64_t entry = ((int64_t)pass * (n + G - 1) + s) * G + t;
+                reinterpret_cast<uint32_t *>(planes)[entry] = tw;
+              }
+            }
           }
         }
       }
+      cp_async_wait_all();
       __syncwarp();
 
       if (gact) {
@@ -368,13 +444,11 @@ __global__ void __launch_bounds__(kThreads) fill_i32_kernel(const FillArgs A) {
     }
 
     // ---- results ------------------------------------------------------
-    const unsigned gm = group_mask<G>(lane);
-    const bool gbad = (__ballot_sync(0xffffffffu, bad) & gm) != 0;
     if constexpr (LOCAL) {
       // First cell in row-major order holding the maximum: largest value,
       // then smallest row, then smallest column.
-      uint64_t key = (uint64_t(uint32_t(lbest)) << 40) | (uint64_t(0xFFFFFu - uint32_t(lrow)) << 20) |
-                     uint64_t(0xFFFFFu - uint32_t(lcol));
+      const uint64_t key = (uint64_t(uint32_t(lbest)) << 40) | (uint64_t(0xFFFFFu - uint32_t(lrow)) << 20) |
+                           uint64_t(0xFFFFFu - uint32_t(lcol));
       const uint64_t gkey = group_max<G>(key);
       const bool owner = (key == gkey) && lbest > 0;
       // Counts of the winning cell travel with the owner.
@@ -398,7 +472,7 @@ __global__ void __launch_bounds__(kThreads) fill_i32_kernel(const FillArgs A) {
         }
       }
     } else {
-      const int owner_t = trivial ? 0 : ((m - 1) % P) / R;
+      const int owner_t = (m > 0) ? ((m - 1) % P) / R : 0;
       const int32_t h = __shfl_sync(0xffffffffu, last_h, gw * G + owner_t);
       const uint32_t c = __shfl_sync(0xffffffffu, last_c, gw * G + owner_t);
       if (have && t == 0) {
@@ -408,7 +482,7 @@ __global__ void __launch_bounds__(kThreads) fill_i32_kernel(const FillArgs A) {
         o.a_end = m;
         o.b_begin = 0;
         o.b_end = n;
-        if (trivial) {
+        if (m == 0 || n == 0) {
           o.score = (m + n == 0) ? 0 : -(go + (m + n) * ge);
           o.n_ident = OUT == kOutScore ? -1 : 0;
           o.n_cols = OUT == kOutScore ? -1 : m + n;
@@ -424,6 +498,39 @@ __global__ void __launch_bounds__(kThreads) fill_i32_kernel(const FillArgs A) {
       }
     }
     __syncwarp();
+  }
+}
+
+// Residency target per SM: 2 blocks (16 warps) for score and traceback
+// fills; identity fills carry path counts and take what they need.
+template <int OUT>
+struct MinBlocks {
+  static constexpr int value = OUT == kOutIdent ? 1 : 2;
+};
+
+template <int R, bool LOCAL, int OUT>
+__global__ void __launch_bounds__(kThreads, MinBlocks<OUT>::value) fill_i32_kernel(const FillArgs A) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  int8_t *s_mat = reinterpret_cast<int8_t *>(smem);
+  uint2 *s_prof = reinterpret_cast<uint2 *>(smem + kMatBytes);
+  uint8_t *s_rings = smem + kMatBytes + kLetters * kThreads * sizeof(uint2);
+  for (int k = threadIdx.x; k < kLetters * kLetters; k += blockDim.x) s_mat[k] = A.matrix[k];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(A.counter, 1);
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= A.n_wtasks) break;
+    const int2 w = A.wtasks[idx];
+    const int G = w.y >> 16, count = w.y & 0xFFFF;
+    switch (G) {
+      case 4: fill_warp_task<4, R, LOCAL, OUT>(A, s_mat, s_prof, s_rings, w.x, count, warp_id); break;
+      case 8: fill_warp_task<8, R, LOCAL, OUT>(A, s_mat, s_prof, s_rings, w.x, count, warp_id); break;
+      case 16: fill_warp_task<16, R, LOCAL, OUT>(A, s_mat, s_prof, s_rings, w.x, count, warp_id); break;
+      default: fill_warp_task<32, R, LOCAL, OUT>(A, s_mat, s_prof, s_rings, w.x, count, warp_id); break;
+    }
   }
 }
 

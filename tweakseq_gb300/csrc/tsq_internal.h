@@ -56,21 +56,25 @@ struct Shape {
   int G, R, i16;
 };
 
+// A warp task: up to 32/G pairs of one lane width G, processed by one warp
+// (x = first index into the task list, y = (G << 16) | number of pairs).
+// The planner orders warp tasks longest first; warps of one persistent
+// launch pull them from a single counter.
 struct FillArgs {
   const uint8_t *codes;
   const PairDev *pairs;
-  const int32_t *tasks;
-  int32_t n_tasks;
-  int32_t *counter;  // work-queue head, zero before the launch
+  const int32_t *tasks;  // pair ids, grouped by warp task
+  const int2 *wtasks;
+  int32_t n_wtasks;
+  int32_t *counter;      // work-queue head, zero before the launch
   const int8_t *matrix;  // 26*26 device copy of the scheme
   int32_t gap_open, gap_extend;
   ResultDev *res;
-  int32_t *bnd;       // boundary scratch
-  int32_t bnd_cols;   // max_n + 1 over the launch
-  int32_t n_slots;    // number of group slots the scratch holds
-  uint8_t *planes;    // TB planes (kOutTrace)
+  int32_t *bnd;          // boundary scratch: per warp, 8 group rows
+  int32_t bnd_cols;      // entries per group row (max n over the launch, even)
+  uint8_t *planes;       // TB planes (kOutTrace)
   const int64_t *plane_off;  // byte offset of each pair's planes
-  int32_t *overflow;  // int16: per pair flag, set when a lane saturated
+  int32_t *overflow;     // int16: per pair flag, set when a lane saturated
 };
 
 struct WalkArgs {
@@ -95,10 +99,12 @@ void build_lut(const Scheme &s, uint8_t lut[256]);
 
 // Kernel launchers (fill_kernels.cu, walk_kernel.cu, encode in batch.cu).
 // Returns the number of thread blocks a persistent launch of this shape uses.
-int fill_blocks(const Shape &sh, int out_mode, bool local);
-size_t fill_smem_bytes(const Shape &sh);
+// A launch covers every lane width G of one row height R and lane type.
+int fill_blocks(int R, int i16, int out_mode, bool local);
+size_t fill_smem_bytes(int R, int i16, int out_mode);
 int fill_threads();
-cudaError_t launch_fill(const Shape &sh, int out_mode, bool local, const FillArgs &a, int blocks,
+size_t fill_bnd_entry_bytes(int i16, int out_mode);
+cudaError_t launch_fill(int R, int i16, int out_mode, bool local, const FillArgs &a, int blocks,
                         cudaStream_t st);
 bool shape_supported(const Shape &sh, int out_mode, bool local);
 cudaError_t launch_walk(const WalkArgs &a, cudaStream_t st);
