@@ -227,3 +227,41 @@ def test_plain_equals_batch():
         assert (r.score, r.aln_a, r.aln_b, r.a_begin, r.b_begin) == (
             int(bat.table["score"][k]), bat.aln_a[k], bat.aln_b[k], int(bat.table["a_begin"][k]),
             int(bat.table["b_begin"][k]))
+
+
+@pytest.mark.parametrize("local", [False, True])
+def test_int16_overflow_rerun_and_lane_choices(local):
+    """Scores beyond int16: the checked int16x2 fill flags them and the int32
+    re-run makes them exact; pairs at the edge of the proven range stay in
+    int16x2; lane='i16' forces the checked kernel on every pair and
+    lane='i32' the int32 kernel."""
+    rng = np.random.default_rng(31)
+    seqs, pairs = [], []
+    for L in (2900, 2978, 2979, 3100, 3500):  # W:W scores 11 per residue
+        seqs += [b"W" * L, b"W" * L]
+        pairs.append((len(seqs) - 2, len(seqs) - 1))
+    for k in range(40):  # ordinary pairs mixed in
+        a = W.random_protein(rng, int(rng.integers(20, 900))).tobytes()
+        b = W.random_protein(rng, int(rng.integers(20, 900))).tobytes()
+        seqs += [a, b]
+        pairs.append((len(seqs) - 2, len(seqs) - 1))
+    ps = W._pairset_from_lists(seqs, pairs)
+    want = oracle_batch(ps, local, O.MODE_SCORE)
+    mode = "local" if local else "global"
+    for lane in ("auto", "i16", "i32"):
+        got = A.align_batch(ps, mode=mode, output="score", lane=lane)
+        assert_same(got, want, score_fields(local), f"lane {lane}")
+    with A.Batch(ps, mode=mode, output="score", lane="auto") as b:
+        b.run()
+        assert_same(b.results(), want, score_fields(local), "batch")
+        assert b.stats()["rerun_pairs"] >= 3  # 2979, 3100 and 3500 overflow (2978 is flagged too)
+
+
+def test_mixed_lane_types_one_batch():
+    """One batch whose pairs split over int16x2, checked int16x2 and int32:
+    with extend 60 the lower bound only fits int16 for short pairs."""
+    ps = random_pairs(41, 300, 5, 700)
+    for local in (False, True):
+        got = A.align_batch(ps, gap_open=20, gap_extend=60, mode="local" if local else "global", output="score")
+        want = O.batch(ps.seqs, ps.a_off, ps.a_len, ps.b_off, ps.b_len, O.BLOSUM62, 20, 60, local, O.MODE_SCORE)
+        assert_same(got, want, score_fields(local), "mixed")

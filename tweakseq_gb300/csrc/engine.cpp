@@ -82,7 +82,7 @@ constexpr int64_t kMaxLen = (1 << 20) - 1;
 
 }  // namespace
 
-Shape ShapeChooser::pick(int m, int n) const {
+Shape ShapeChooser::pick(int m, int n, int rows_per_lane) const {
   // Lanes per pair G: (1) enough groups to fill every SM about 24 warps
   // deep; (2) enough lanes that this pair's sweep -- about m*n / (G*R)
   // dependent steps -- stays under half the balanced per-lane work of the
@@ -92,10 +92,10 @@ Shape ShapeChooser::pick(int m, int n) const {
   int g_occ = npairs > 0 ? pow2ceil((target_warps * 32 + npairs - 1) / npairs) : 32;
   int g_lat = 1;
   if (avg_lane_steps > 0) {
-    const double steps_at_g1 = double(m) * double(n) / kR;
+    const double steps_at_g1 = double(m) * double(n) / rows_per_lane;
     g_lat = pow2ceil(int64_t(steps_at_g1 / (0.5 * avg_lane_steps)) + 1);
   }
-  const int rows_cap = pow2ceil((m + kR - 1) / kR);
+  const int rows_cap = pow2ceil((m + rows_per_lane - 1) / rows_per_lane);
   int G = std::max(g_occ, g_lat);
   Shape sh{};
   if (use_table && tune_table_pick(out_mode, m, n, &sh) && shape_supported(sh, out_mode, local)) {
@@ -194,6 +194,32 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   }
   b->cells = cells;
 
+  // ---- lane types ------------------------------------------------------
+  // Score fills run in int16x2 when the pair's values provably fit: the
+  // upper bound max_score * min(m, n) (unchecked kernel) and the lower
+  // bound -(3*open + (m + 512 + n + 1)*ext + open + ext + 128 + |min|),
+  // 512 being the most padding rows a pass can add, against the int16
+  // kernels' minus infinity (-32000).  Pairs with the lower bound but not
+  // the upper one run the overflow-checked int16x2 kernel and are re-run
+  // in int32 if flagged; everything else runs in int32.
+  std::vector<int8_t> lsel(static_cast<size_t>(n));
+  int64_t n_checked = 0;
+  for (int64_t k = 0; k < n; ++k) {
+    const PairDev &pd = b->pairs_h[size_t(k)];
+    int8_t lt = 0;
+    if (b->out_mode == kOutScore && p->lane != TSQ_LANE_I32) {
+      const int64_t go = p->gap_open, ge = p->gap_extend;
+      const int64_t lowest = 3 * go + (int64_t(pd.a_len) + 512 + pd.b_len + 1) * ge + go + ge + 128 +
+                             std::max<int64_t>(0, -int64_t(sc.min_score));
+      const bool lower_ok = lowest < 31000 && ge <= 700 && pd.b_len <= 65535;
+      const bool upper_ok =
+          int64_t(std::max(sc.max_score, 0)) * std::min(pd.a_len, pd.b_len) + std::max(sc.max_score, 0) < 32767;
+      if (lower_ok) lt = (upper_ok && p->lane == TSQ_LANE_AUTO) ? 1 : 2;
+    }
+    lsel[size_t(k)] = lt;
+    n_checked += lt == 2;
+  }
+
   // ---- shapes and buckets ----------------------------------------------
   ShapeChooser ch;
   ch.out_mode = b->out_mode;
@@ -209,78 +235,120 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   std::vector<int32_t> rsel(static_cast<size_t>(n));
   std::vector<int32_t> order(static_cast<size_t>(n));
   for (int64_t k = 0; k < n; ++k) {
-    const Shape s = ch.pick(b->pairs_h[size_t(k)].a_len, b->pairs_h[size_t(k)].b_len);
+    const int rows_per_lane = lsel[size_t(k)] ? 2 * kR : kR;
+    Shape s = ch.pick(b->pairs_h[size_t(k)].a_len, b->pairs_h[size_t(k)].b_len, rows_per_lane);
+    s.i16 = 0;
     if (!shape_supported(s, b->out_mode, b->local)) return TSQ_E_INVALID_ARG;
     gsel[size_t(k)] = s.G;
     rsel[size_t(k)] = s.R;
     order[size_t(k)] = int32_t(k);
   }
+  // Bands and steps of a pair's sweep under its lane type and shape.
   auto bands = [&](int32_t k) {
-    const int P = gsel[size_t(k)] * rsel[size_t(k)];
+    const int P = gsel[size_t(k)] * rsel[size_t(k)] * (lsel[size_t(k)] ? 2 : 1);
     return (b->pairs_h[size_t(k)].a_len + P - 1) / P;
   };
+  auto steps = [&](int32_t k) {
+    return b->pairs_h[size_t(k)].b_len + gsel[size_t(k)] * (lsel[size_t(k)] ? 2 : 1) - 1;
+  };
   std::sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+    if (lsel[size_t(x)] != lsel[size_t(y)]) return lsel[size_t(x)] > lsel[size_t(y)];
     if (gsel[size_t(x)] != gsel[size_t(y)]) return gsel[size_t(x)] < gsel[size_t(y)];
-    if (rsel[size_t(x)] != rsel[size_t(y)]) return rsel[size_t(x)] < rsel[size_t(y)];
     const int bx = bands(x), by = bands(y);
     if (bx != by) return bx > by;
     const int nx = b->pairs_h[size_t(x)].b_len, ny = b->pairs_h[size_t(y)].b_len;
     if (nx != ny) return nx > ny;
     return x < y;
   });
-  // Warp tasks: consecutive pairs of one bucket, 32/G per warp; their cost
-  // is the longest sweep among them (bands x steps).  Longest first.
-  std::vector<int2> wt;
-  std::vector<int64_t> wcost;
+
+  // One launch per lane type (int16x2 checked, int16x2, int32), each a list
+  // of warp tasks -- consecutive pairs of one lane width, 32/G per warp --
+  // ordered by cost (bands x steps of the longest pair), longest first.
+  b->launches.clear();
+  std::vector<int2> wt_all;
+  int64_t bnd_total = 0;
+  int32_t checked_begin = 0;
   for (int64_t s = 0; s < n;) {
-    const int32_t k0 = order[size_t(s)];
-    const int G = gsel[size_t(k0)];
-    const int per = 32 / G;
+    const int8_t lt = lsel[size_t(order[size_t(s)])];
     int64_t e = s;
-    int64_t cost = 0;
-    while (e < n && e - s < per && gsel[size_t(order[size_t(e)])] == G) {
-      const int32_t k = order[size_t(e)];
-      cost = std::max<int64_t>(cost, int64_t(bands(k)) * (b->pairs_h[size_t(k)].b_len + G - 1));
+    int32_t cols = 1;
+    while (e < n && lsel[size_t(order[size_t(e)])] == lt) {
+      cols = std::max(cols, b->pairs_h[size_t(order[size_t(e)])].b_len);
       ++e;
     }
-    wt.push_back(make_int2(int32_t(s), (G << 16) | int32_t(e - s)));
-    wcost.push_back(cost);
-    s = e;
-  }
-  std::vector<int32_t> worder(wt.size());
-  std::iota(worder.begin(), worder.end(), 0);
-  std::stable_sort(worder.begin(), worder.end(), [&](int32_t x, int32_t y) { return wcost[size_t(x)] > wcost[size_t(y)]; });
-  std::vector<int2> wt_sorted(wt.size());
-  for (size_t k = 0; k < wt.size(); ++k) wt_sorted[k] = wt[size_t(worder[k])];
-
-  b->launches.clear();
-  int64_t bnd_total = 0;
-  if (!wt_sorted.empty()) {
+    if (lt == 2) checked_begin = int32_t(s);
+    std::vector<int2> wt;
+    std::vector<int64_t> wcost;
+    for (int64_t q = s; q < e;) {
+      const int G = gsel[size_t(order[size_t(q)])];
+      const int per = 32 / G;
+      int64_t r = q;
+      int64_t cost = 0;
+      while (r < e && r - q < per && gsel[size_t(order[size_t(r)])] == G) {
+        const int32_t k = order[size_t(r)];
+        cost = std::max<int64_t>(cost, int64_t(bands(k)) * steps(k));
+        ++r;
+      }
+      wt.push_back(make_int2(int32_t(q), (G << 16) | int32_t(r - q)));
+      wcost.push_back(cost);
+      q = r;
+    }
+    std::vector<int32_t> worder(wt.size());
+    std::iota(worder.begin(), worder.end(), 0);
+    std::stable_sort(worder.begin(), worder.end(),
+                     [&](int32_t x, int32_t y) { return wcost[size_t(x)] > wcost[size_t(y)]; });
     Launch L;
     L.R = kR;
-    L.i16 = 0;
-    L.wt_begin = 0;
-    L.n_wtasks = int32_t(wt_sorted.size());
+    L.i16 = lt;
+    L.wt_begin = int32_t(wt_all.size());
+    L.n_wtasks = int32_t(wt.size());
+    for (int32_t w : worder) wt_all.push_back(wt[size_t(w)]);
     const int max_blocks = fill_blocks(L.R, L.i16, b->out_mode, b->local);
     if (max_blocks <= 0) return TSQ_E_CUDA;
-    const int warps_per_block = fill_threads() / 32;
+    const int warps_per_block = fill_threads_for(L.i16) / 32;
     const int64_t needed = (int64_t(L.n_wtasks) + warps_per_block - 1) / warps_per_block;
     L.blocks = int32_t(std::max<int64_t>(1, std::min<int64_t>(max_blocks, needed)));
     // Whole staged chunks are copied, so rows are padded to a chunk past n.
-    L.bnd_cols = ((max_n + 31) / 32 + 1) * 32;
-    L.bnd_offset = 0;
-    bnd_total = int64_t(L.blocks) * warps_per_block * 8 * L.bnd_cols *
-                int64_t(fill_bnd_entry_bytes(L.i16, b->out_mode));
+    L.bnd_cols = ((cols + 31) / 32 + 1) * 32;
+    L.bnd_offset = bnd_total;
+    bnd_total += int64_t(L.blocks) * warps_per_block * 8 * L.bnd_cols *
+                 int64_t(fill_bnd_entry_bytes(L.i16, b->out_mode));
+    bnd_total = (bnd_total + 255) & ~int64_t(255);
+    b->launches.push_back(L);
+    s = e;
+  }
+  // The int32 re-run of pairs the checked int16x2 launch flags: its warp
+  // tasks are built on the device, its size bounded by the checked pairs.
+  b->n_checked = n_checked;
+  b->checked_begin = checked_begin;
+  if (n_checked > 0) {
+    int32_t cols = 1;
+    for (int64_t q = checked_begin; q < checked_begin + n_checked; ++q)
+      cols = std::max(cols, b->pairs_h[size_t(order[size_t(q)])].b_len);
+    Launch L;
+    L.R = kR;
+    L.i16 = 0;
+    L.rerun = true;
+    const int max_blocks = fill_blocks(L.R, 0, b->out_mode, b->local);
+    if (max_blocks <= 0) return TSQ_E_CUDA;
+    const int warps_per_block = fill_threads_for(0) / 32;
+    L.blocks = int32_t(std::max<int64_t>(1, std::min<int64_t>(max_blocks, (n_checked + warps_per_block - 1) /
+                                                                             warps_per_block)));
+    L.bnd_cols = ((cols + 31) / 32 + 1) * 32;
+    L.bnd_offset = bnd_total;
+    bnd_total += int64_t(L.blocks) * warps_per_block * 8 * L.bnd_cols * int64_t(fill_bnd_entry_bytes(0, b->out_mode));
     b->launches.push_back(L);
   }
   b->stats.pairs = n;
   b->stats.cells = cells;
-  b->stats.launches = int32_t(b->launches.size()) + 1 + (b->out_mode == kOutTrace ? 1 : 0);
+  b->stats.launches = int32_t(b->launches.size()) + 1 + (b->out_mode == kOutTrace ? 1 : 0) + (n_checked > 0 ? 1 : 0);
   {
-    std::vector<int32_t> gs(gsel);
+    std::vector<int32_t> gs;
+    for (int64_t k = 0; k < n; ++k) gs.push_back(gsel[size_t(k)] * 4 + lsel[size_t(k)]);
     std::sort(gs.begin(), gs.end());
     b->stats.buckets = int32_t(std::unique(gs.begin(), gs.end()) - gs.begin());
   }
+  const std::vector<int2> &wt_sorted = wt_all;
 
   // ---- traceback layout ----------------------------------------------------
   std::vector<int64_t> ploff;
@@ -310,7 +378,15 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   TSQ_TRY(b->res.ensure(sizeof(ResultDev) * size_t(n)));
   TSQ_TRY(b->bnd.ensure(size_t(bnd_total)));
   TSQ_TRY(b->wtasks.ensure(sizeof(int2) * std::max<size_t>(1, wt_sorted.size())));
-  TSQ_TRY(b->counters.ensure(sizeof(int32_t) * (b->launches.size() + 1)));
+  TSQ_TRY(b->counters.ensure(sizeof(int32_t) * (b->launches.size() + 2)));
+  TSQ_TRY(b->shape_g.ensure(sizeof(int32_t) * size_t(n)));
+  TSQ_TRY(b->shape_r.ensure(sizeof(int32_t) * size_t(n)));
+  if (n_checked > 0) {
+    TSQ_TRY(b->overflow.ensure(sizeof(int32_t) * size_t(n)));
+    TSQ_TRY(b->rerun_tasks.ensure(sizeof(int32_t) * size_t(n_checked)));
+    TSQ_TRY(b->rerun_wtasks.ensure(sizeof(int2) * size_t(n_checked)));
+  }
+  TSQ_TRY(b->rerun_h.ensure(sizeof(int32_t)));
   TSQ_TRY(b->lut.ensure(256));
   TSQ_TRY(b->matrix.ensure(kLetters * kLetters));
   TSQ_TRY(b->res_h.ensure(sizeof(ResultDev) * size_t(n)));
@@ -319,8 +395,6 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
     TSQ_TRY(b->plane_off.ensure(sizeof(int64_t) * size_t(n)));
     TSQ_TRY(b->aln.ensure(size_t(b->aln_bytes)));
     TSQ_TRY(b->aln_off.ensure(sizeof(int64_t) * size_t(n)));
-    TSQ_TRY(b->shape_g.ensure(sizeof(int32_t) * size_t(n)));
-    TSQ_TRY(b->shape_r.ensure(sizeof(int32_t) * size_t(n)));
     TSQ_TRY(b->aln_h.ensure(size_t(b->aln_bytes)));
   }
   cudaStream_t st = b->stream;
@@ -337,6 +411,8 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
     TSQ_TRY(cudaMemcpyAsync(b->plane_off.p, ploff.data(), sizeof(int64_t) * size_t(n), cudaMemcpyHostToDevice, st));
     TSQ_TRY(cudaMemcpyAsync(b->aln_off.p, b->aln_off_h.data(), sizeof(int64_t) * size_t(n), cudaMemcpyHostToDevice,
                             st));
+  }
+  if (n > 0) {
     TSQ_TRY(cudaMemcpyAsync(b->shape_g.p, gsel.data(), sizeof(int32_t) * size_t(n), cudaMemcpyHostToDevice, st));
     TSQ_TRY(cudaMemcpyAsync(b->shape_r.p, rsel.data(), sizeof(int32_t) * size_t(n), cudaMemcpyHostToDevice, st));
   }
@@ -357,18 +433,26 @@ cudaError_t record(tsq_batch *b, int k) {
 int enqueue_run(tsq_batch *b) {
   cudaStream_t st = b->stream;
   const int nl = int(b->launches.size());
-  TSQ_TRY(cudaMemsetAsync(b->counters.p, 0, sizeof(int32_t) * (size_t(nl) + 1), st));
+  TSQ_TRY(cudaMemsetAsync(b->counters.p, 0, sizeof(int32_t) * (size_t(nl) + 2), st));
   TSQ_TRY(record(b, 0));
   TSQ_TRY(launch_encode(b->seqs.as<uint8_t>(), b->seqs_len, b->lut.as<uint8_t>(), b->codes.as<uint8_t>(), st));
   TSQ_TRY(record(b, 1));
+  int32_t *rerun_count = b->counters.as<int32_t>() + nl + 1;
   for (int l = 0; l < nl; ++l) {
     const Launch &L = b->launches[size_t(l)];
+    if (L.rerun) {
+      // Pairs the checked int16x2 launch flagged, compacted on the device.
+      TSQ_TRY(launch_collect_overflow(b->tasks.as<int32_t>() + b->checked_begin, int32_t(b->n_checked),
+                                      b->overflow.as<int32_t>(), b->shape_g.as<int32_t>(),
+                                      b->rerun_tasks.as<int32_t>(), b->rerun_wtasks.as<int2>(), rerun_count, st));
+    }
     FillArgs a{};
     a.codes = b->codes.as<uint8_t>();
     a.pairs = b->pairs.as<PairDev>();
-    a.tasks = b->tasks.as<int32_t>();
-    a.wtasks = b->wtasks.as<int2>() + L.wt_begin;
+    a.tasks = L.rerun ? b->rerun_tasks.as<int32_t>() : b->tasks.as<int32_t>();
+    a.wtasks = L.rerun ? b->rerun_wtasks.as<int2>() : b->wtasks.as<int2>() + L.wt_begin;
     a.n_wtasks = L.n_wtasks;
+    a.n_wtasks_dev = L.rerun ? rerun_count : nullptr;
     a.counter = b->counters.as<int32_t>() + l;
     a.matrix = b->matrix.as<int8_t>();
     a.gap_open = b->params.gap_open;
@@ -378,9 +462,12 @@ int enqueue_run(tsq_batch *b) {
     a.bnd_cols = L.bnd_cols;
     a.planes = b->planes.as<uint8_t>();
     a.plane_off = b->plane_off.as<int64_t>();
-    a.overflow = nullptr;
+    a.overflow = b->overflow.as<int32_t>();
+    a.max_score = b->scheme.max_score;
     TSQ_TRY(launch_fill(L.R, L.i16, b->out_mode, b->local, a, L.blocks, st));
   }
+  if (b->n_checked > 0)
+    TSQ_TRY(cudaMemcpyAsync(b->rerun_h.p, rerun_count, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   TSQ_TRY(record(b, 2));
   if (b->out_mode == kOutTrace) {
     WalkArgs w{};
@@ -439,6 +526,7 @@ int batch_sync(tsq_batch *b) {
   if (!b) return TSQ_E_INVALID_ARG;
   TSQ_TRY(cudaStreamSynchronize(b->stream));
   if (!b->has_run) return TSQ_OK;
+  b->stats.rerun_pairs = b->n_checked > 0 ? *b->rerun_h.as<int32_t>() : 0;
   float total = 0.f, fill = 0.f;
   if (cudaEventElapsedTime(&total, b->ev[0], b->ev[3]) == cudaSuccess) {
     b->stats.device_ms = total;

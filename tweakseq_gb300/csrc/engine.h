@@ -44,7 +44,8 @@ struct PinBuf {
 // One persistent fill launch: every warp task of one row height R and lane
 // type, all lane widths G mixed, longest first.
 struct Launch {
-  int R = 8, i16 = 0;
+  int R = 8, i16 = 0;  // i16: 0 int32, 1 int16x2, 2 int16x2 with overflow check
+  bool rerun = false;  // int32 re-run of flagged pairs (warp tasks built on the device)
   int32_t wt_begin = 0, n_wtasks = 0;  // slice of the warp-task list
   int32_t blocks = 0;
   int32_t bnd_cols = 0;
@@ -62,7 +63,7 @@ struct ShapeChooser {
   // more than about half of it, or it becomes the batch's tail.
   double avg_lane_steps = 0.0;
   bool use_table = false;
-  Shape pick(int m, int n) const;
+  Shape pick(int m, int n, int rows_per_lane) const;
 };
 
 bool tune_table_loaded();
@@ -94,8 +95,10 @@ struct tsq_batch {
   bool has_run = false;
 
   tsq::DevBuf seqs, codes, pairs, tasks, wtasks, res, bnd, planes, plane_off, aln, aln_off, shape_g, shape_r, counters,
-      lut, matrix;
-  tsq::PinBuf res_h, aln_h;
+      lut, matrix, overflow, rerun_tasks, rerun_wtasks;
+  tsq::PinBuf res_h, aln_h, rerun_h;
+  int64_t n_checked = 0;
+  int32_t checked_begin = 0;
 
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;

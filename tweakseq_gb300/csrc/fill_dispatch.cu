@@ -1,4 +1,5 @@
 // fill_dispatch.cu -- picks the fill kernel for an output mode and lane type.
+#include "fill_i16.cuh"
 #include "fill_i32.cuh"
 
 namespace tsq {
@@ -7,35 +8,41 @@ template <int OUT>
 cudaError_t launch_i32(bool local, const FillArgs &a, int blocks, size_t smem, cudaStream_t st);
 template <int OUT>
 int occupancy_i32(bool local, size_t smem);
+cudaError_t launch_i16(bool check, bool local, const FillArgs &a, int blocks, size_t smem, cudaStream_t st);
+int occupancy_i16(bool check, bool local, size_t smem);
+size_t smem_i16();
 }  // namespace fill
 
 int fill_threads() { return fill::kThreads; }
 
 size_t fill_smem_bytes(int R, int i16, int out_mode) {
-  (void)i16;
+  if (i16) return fill::smem_i16();
   const size_t top = out_mode == kOutIdent ? 16 : 8;
   return size_t(fill::kMatBytes) + size_t(kLetters) * fill::kThreads * size_t(R) +
-         size_t(fill::kSlotsPerBlock) * (fill::kTopRing * top + fill::kCodeRing);
+         size_t(fill::kSlotsPerBlock) * (fill::kTopRing * top + fill::kCodeRing + 2 * fill::kRingPad);
 }
 
 size_t fill_bnd_entry_bytes(int i16, int out_mode) {
-  (void)i16;
+  if (i16) return 4;
   return out_mode == kOutIdent ? 16 : 8;
 }
 
+int fill_threads_for(int i16) { return i16 ? fill::kThreads16 : fill::kThreads; }
+
 bool shape_supported(const Shape &sh, int out_mode, bool local) {
   (void)local;
-  (void)out_mode;
-  if (sh.i16 || sh.R != 8) return false;
+  if (sh.R != 8) return false;
+  if (sh.i16 && out_mode != kOutScore) return false;
   return sh.G == 4 || sh.G == 8 || sh.G == 16 || sh.G == 32;
 }
 
 int fill_blocks(int R, int i16, int out_mode, bool local) {
-  if (R != 8 || i16) return 0;
+  if (R != 8) return 0;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const size_t smem = fill_smem_bytes(R, i16, out_mode);
+  if (i16) return out_mode == kOutScore ? fill::occupancy_i16(i16 == 2, local, smem) * sms : 0;
   int per_sm = 0;
   switch (out_mode) {
     case kOutScore: per_sm = fill::occupancy_i32<kOutScore>(local, smem); break;
@@ -47,8 +54,12 @@ int fill_blocks(int R, int i16, int out_mode, bool local) {
 
 cudaError_t launch_fill(int R, int i16, int out_mode, bool local, const FillArgs &a, int blocks,
                         cudaStream_t st) {
-  if (R != 8 || i16) return cudaErrorInvalidValue;
+  if (R != 8) return cudaErrorInvalidValue;
   const size_t smem = fill_smem_bytes(R, i16, out_mode);
+  if (i16) {
+    if (out_mode != kOutScore) return cudaErrorInvalidValue;
+    return fill::launch_i16(i16 == 2, local, a, blocks, smem, st);
+  }
   switch (out_mode) {
     case kOutScore: return fill::launch_i32<kOutScore>(local, a, blocks, smem, st);
     case kOutIdent: return fill::launch_i32<kOutIdent>(local, a, blocks, smem, st);

@@ -1,0 +1,388 @@
+// fill_i16.cuh -- group-striped Gotoh fill, score only, in packed int16x2
+// with DPX instructions (two cells per instruction).
+//
+// Same recurrences and work split as the int32 fill (fill_i32.cuh), with two
+// row bands per pass packed into the two 16-bit halves of every register:
+// lane t holds rows t*R .. t*R+R-1 of band A in the low halves and the same
+// rows of band B (the G*R rows below band A) in the high halves.  Band B
+// runs G columns behind band A, so at step s lane t computes column s - t of
+// band A and column s - t - G of band B.  One rotate-shuffle per value
+// carries each lane's bottom row to the next lane; lane 0 gets band A's top
+// row from the staged top-row ring and band B's top row from lane G-1's
+// band-A bottom row, which is exactly one step old.  Only the bottom row of
+// band B goes back to HBM.
+//
+// Per packed cell the fill issues 7 instructions: the profile PRMT that
+// builds the two int16 scores and six DPX add/max forms -- E = max(E - ext,
+// T), X = max(D + s, E), F = max(F_above - ext, XO_above), H = max(X, F),
+// T = H - (open + ext) for the next column's E, and XO = X - (open + ext)
+// (X clamped at 0 first in local mode) for the next row's F.  F can take X
+// instead of H from the row above because open >= 0 makes the F - open - ext
+// candidate redundant, so rows depend on each other through one add-max
+// only.
+//
+// Range.  The planner only sends a pair here when every value of its matrix
+// fits int16: H <= max_score * min(m, n) and every H, E, F >= -(3*open +
+// (rows + n + 1)*ext + 128), checked on the host against kNeg16.  Pairs
+// whose upper bound is not proven run the CHECK variant, which keeps the
+// running maximum of H and flags the pair for an exact int32 re-run when it
+// comes within max_score of 32767 (an overflow must pass through such a
+// value first, since one diagonal step adds at most max_score).
+#pragma once
+
+#include <cstdint>
+
+#include "fill_common.cuh"
+
+namespace tsq {
+namespace fill {
+
+constexpr int kThreads16 = 128;  // 4 warps per block: the profile is 416 bytes per thread
+constexpr int kSlots16 = kThreads16 / 32 * 8;
+constexpr int kCodeRing16 = 256;  // band B reads codes up to 2G columns behind band A
+constexpr int32_t kNeg16 = -32000;
+constexpr uint32_t kNeg2 = 0x83008300u;  // kNeg16 in both halves
+
+__device__ __forceinline__ uint32_t pack2(int32_t lo, int32_t hi) {
+  return (uint32_t(lo) & 0xFFFFu) | (uint32_t(hi) << 16);
+}
+
+// (sign-extended byte K of a, sign-extended byte K of b) as int16x2.
+template <int K>
+__device__ __forceinline__ uint32_t score2(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "n"(K | ((K | 8) << 4) | ((4 + K) << 8) | ((12 + K) << 12)));
+  return d;
+}
+
+__device__ __forceinline__ uint32_t score2_dyn(uint32_t a, uint32_t b, int k) {
+  switch (k & 3) {
+    case 0: return score2<0>(a, b);
+    case 1: return score2<1>(a, b);
+    case 2: return score2<2>(a, b);
+    default: return score2<3>(a, b);
+  }
+}
+
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
+  uint32_t d;
+  asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(sel));
+  return d;
+}
+
+template <bool B>
+struct BoolTag {
+  static constexpr bool value = B;
+};
+
+// The lane width G is a run-time value: one code path serves every width,
+// which keeps the kernel small enough for the instruction cache.
+template <bool LOCAL, bool CHECK>
+__device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t *s_mat, uint2 *s_prof,
+                                                 uint8_t *s_rings, int begin, int count, int warp_id, int G,
+                                                 int lg) {
+  constexpr int R = 8;
+  const int P = G * R;   // rows per band
+  const int P2 = 2 * P;  // rows per pass (bands A and B)
+  const int lane = threadIdx.x & 31;
+  const int t = lane & (G - 1);
+  const int gw = lane >> lg;
+  const int32_t go = A.gap_open, ge = A.gap_extend, oe = go + ge;
+  const uint32_t nge2 = pack2(-ge, -ge), noe2 = pack2(-oe, -oe);
+  uint32_t *top = reinterpret_cast<uint32_t *>(A.bnd) + ((int64_t)warp_id * 8 + gw) * A.bnd_cols;
+  const int gslot = (threadIdx.x >> 5) * 8 + gw;
+  constexpr int kTopStride = kTopRing * 4 + kRingPad;  // bytes
+  uint32_t *top_ring = reinterpret_cast<uint32_t *>(s_rings + gslot * kTopStride);
+  uint8_t *code_ring = s_rings + kSlots16 * kTopStride + gslot * (kCodeRing16 + kRingPad);
+  const uint2 *profA = s_prof + threadIdx.x;                // + (2c) * kThreads16
+  const uint2 *profB = s_prof + kThreads16 + threadIdx.x;   // + (2c) * kThreads16
+  const int src_lane = (lane & ~(G - 1)) | ((t + G - 1) & (G - 1));  // rotate within the group
+
+  const bool have = gw < count;
+  const int pid = have ? A.tasks[begin + gw] : 0;
+  int m = 0, n = 0;
+  const uint8_t *qa_codes = A.codes;
+  int64_t boff = 0;
+  if (have) {
+    const PairDev pr = A.pairs[pid];
+    m = pr.a_len;
+    n = pr.b_len;
+    qa_codes = A.codes + pr.a_off;
+    boff = pr.b_off;
+  }
+  const uint8_t *qb_codes = A.codes + boff;
+  bool bad = false;
+  for (int k = t; k < m; k += G) bad |= qa_codes[k] >= kLetters;
+  for (int k = t; k < n; k += G) bad |= qb_codes[k] >= kLetters;
+  const unsigned gm = group_mask_rt(lane, G);
+  const bool gbad = (__ballot_sync(0xffffffffu, bad) & gm) != 0;
+  const bool trivial = (m == 0 || n == 0 || gbad);
+  const int passes = trivial ? 0 : (m + P2 - 1) / P2;
+  const int steps = trivial ? 0 : n + 2 * G - 1;
+  int max_passes = passes, max_steps = steps;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    max_passes = max(max_passes, __shfl_xor_sync(0xffffffffu, max_passes, o));
+    max_steps = max(max_steps, __shfl_xor_sync(0xffffffffu, max_steps, o));
+  }
+
+  // Row 0 of the matrix becomes the first top row: (H, F) as int16 halves.
+  if (!trivial)
+    for (int j = t; j < n; j += G) top[j] = pack2(edge_h(j + 1, go, ge, LOCAL), kNeg16);
+  __syncwarp();
+
+  int32_t lbest = 0, lrow = 0, lcol = 0;
+  int32_t last_h = 0;
+  uint32_t hmax = LOCAL ? 0u : kNeg2;
+
+  for (int pass = 0; pass < max_passes; ++pass) {
+    const bool gact = pass < passes;
+    const int nact = gact ? n : 0;
+    const int rowA = pass * P2 + t * R;  // band A rows rowA+1 .. rowA+R (1-based)
+    const int rowB = rowA + P;           // band B rows rowB+1 .. rowB+R
+    // Profile of this lane's 16 rows (padding rows score 0).
+    {
+      int qa[R], qb[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        qa[r] = (gact && rowA + r < m) ? int(qa_codes[rowA + r]) : -1;
+        qb[r] = (gact && rowB + r < m) ? int(qa_codes[rowB + r]) : -1;
+      }
+#pragma unroll 2
+      for (int c = 0; c < kLetters; ++c) {
+        uint32_t wa[2], wb[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          uint32_t va = 0, vb = 0;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const int xa = qa[q * 4 + k], xb = qb[q * 4 + k];
+            va |= (xa >= 0 ? uint32_t(uint8_t(s_mat[xa * kLetters + c])) : 0u) << (8 * k);
+            vb |= (xb >= 0 ? uint32_t(uint8_t(s_mat[xb * kLetters + c])) : 0u) << (8 * k);
+          }
+          wa[q] = va;
+          wb[q] = vb;
+        }
+        s_prof[(2 * c) * kThreads16 + threadIdx.x] = make_uint2(wa[0], wa[1]);
+        s_prof[(2 * c + 1) * kThreads16 + threadIdx.x] = make_uint2(wb[0], wb[1]);
+      }
+    }
+
+    uint32_t H[R], E[R], T[R];
+    uint32_t best[R], bcol[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      H[r] = pack2(edge_h(rowA + r + 1, go, ge, LOCAL), edge_h(rowB + r + 1, go, ge, LOCAL));
+      T[r] = __viaddmax_s16x2(H[r], noe2, kNeg2);
+      E[r] = kNeg2;
+      best[r] = 0u;
+      bcol[r] = 0u;
+    }
+    uint32_t hdiag = pack2(edge_h(rowA, go, ge, LOCAL), edge_h(rowB, go, ge, LOCAL));
+    uint32_t outH = 0u, outF = kNeg2;
+
+    cp_async_wait_all();
+    __syncwarp();
+    stage_chunk_rt<uint32_t, kCodeRing16>(G, 0, t, nact, top, top_ring, A.codes, boff, code_ring);
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncwarp();
+    stage_chunk_rt<uint32_t, kCodeRing16>(G, 1, t, nact, top, top_ring, A.codes, boff, code_ring);
+    cp_async_commit();
+
+    uint2 pa[2], pb[2];
+    uint32_t tv[2];
+    {
+      const int ca = min(int(code_ring[(boff - t) & (kCodeRing16 - 1)]), kLetters - 1);
+      const int cb = min(int(code_ring[(boff - t - G) & (kCodeRing16 - 1)]), kLetters - 1);
+      pa[0] = profA[(2 * ca) * kThreads16];
+      pb[0] = profB[(2 * cb) * kThreads16];
+      tv[0] = top_ring[0];
+    }
+
+    for (int s0 = 0; s0 < max_steps; s0 += 2) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int s = s0 + k;
+        if (s < max_steps) {
+          if (((s + 1) & (kChunk - 1)) == 0) {
+            cp_async_wait_all();
+            __syncwarp();
+            stage_chunk_rt<uint32_t, kCodeRing16>(G, (s + 1) / kChunk + 1, t, nact, top, top_ring, A.codes, boff,
+                                                  code_ring);
+            cp_async_commit();
+          }
+          const uint32_t rH = __shfl_sync(0xffffffffu, outH, src_lane);
+          const uint32_t rF = __shfl_sync(0xffffffffu, outF, src_lane);
+          const int jA = s - t, jB = jA - G;
+          const bool vA = (unsigned)jA < (unsigned)nact;
+          const bool vB = (unsigned)jB < (unsigned)nact;
+          const uint2 wa = pa[k & 1], wb = pb[k & 1];
+          {
+            const int ca = min(int(code_ring[(boff + jA + 1) & (kCodeRing16 - 1)]), kLetters - 1);
+            const int cb = min(int(code_ring[(boff + jB + 1) & (kCodeRing16 - 1)]), kLetters - 1);
+            pa[(k + 1) & 1] = profA[(2 * ca) * kThreads16];
+            pb[(k + 1) & 1] = profB[(2 * cb) * kThreads16];
+          }
+          uint32_t upH = rH, upF = rF;
+          if (t == 0) {
+            // Band A: the staged top row; band B: lane G-1's band-A bottom.
+            upH = prmt(tv[k & 1], rH, 0x5410u);
+            upF = prmt(tv[k & 1], rF, 0x5432u);
+            tv[(k + 1) & 1] = top_ring[(jA + 1) & (kTopRing - 1)];
+          }
+          if (vA || vB) {
+            // Halves outside their column range keep their old values.
+            const uint32_t keep = (vA ? 0u : 0x0000FFFFu) | (vB ? 0u : 0xFFFF0000u);
+            // A half that has not started keeps its left-boundary diagonal.
+            uint32_t d = hdiag;
+            hdiag = keep ? ((upH & ~keep) | (hdiag & keep)) : upH;
+            // F of the lane's first row from the row above it.
+            uint32_t fv = __viaddmax_s16x2(upF, nge2, __viaddmax_s16x2(upH, noe2, kNeg2));
+            uint32_t xo = 0u;
+            // Rows in order.  Since open >= 0, F(i+1,j) = max(F(i,j) - ext,
+            // max(X(i,j) [, 0]) - open - ext) with X = max(D + s, E): the
+            // only dependence between rows is one add-max on F.
+            auto sweep = [&](auto masked_tag) {
+              constexpr bool MASKED = decltype(masked_tag)::value;
+#pragma unroll
+              for (int r = 0; r < R; ++r) {
+                const uint32_t sc = score2_dyn(r < 4 ? wa.x : wa.y, r < 4 ? wb.x : wb.y, r);
+                uint32_t e = __viaddmax_s16x2(E[r], nge2, T[r]);
+                const uint32_t x = __viaddmax_s16x2(d, sc, e);
+                const uint32_t f = r == 0 ? fv : __viaddmax_s16x2(fv, nge2, xo);
+                uint32_t h = LOCAL ? __vimax_s16x2_relu(x, f) : __vimax3_s16x2(x, f, f);
+                uint32_t tn = __viaddmax_s16x2(h, noe2, kNeg2);
+                xo = LOCAL ? __viaddmax_s16x2(x, noe2, noe2) : __viaddmax_s16x2(x, noe2, kNeg2);
+                if constexpr (MASKED) {
+                  h = (h & ~keep) | (H[r] & keep);
+                  tn = (tn & ~keep) | (T[r] & keep);
+                  e = (e & ~keep) | (E[r] & keep);
+                }
+                if constexpr (CHECK) hmax = __vimax3_s16x2(hmax, h, h);
+                if constexpr (LOCAL) {
+                  // Halves where this cell beats the row's best so far
+                  // (strictly, so the first column of a maximum is kept).
+                  const uint32_t cm = __vcmpgts2(h, best[r]);
+                  best[r] = __vimax3_s16x2(best[r], h, h);
+                  bcol[r] = (bcol[r] & ~cm) | (pack2(jA + 1, jB + 1) & cm);
+                }
+                d = H[r];
+                H[r] = h;
+                T[r] = tn;
+                E[r] = e;
+                fv = f;
+              }
+            };
+            if (keep == 0u)
+              sweep(BoolTag<false>{});
+            else
+              sweep(BoolTag<true>{});
+            outH = H[R - 1];
+            outF = fv;
+            if (t == G - 1 && vB) top[jB] = prmt(outH, outF, 0x7632u);
+          }
+        }
+      }
+    }
+    cp_async_wait_all();
+    __syncwarp();
+
+    if (gact) {
+      if constexpr (LOCAL) {
+        // Band A rows of this pass precede band B rows; within a band rows
+        // increase with r, so strict comparisons keep the first maximum.
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const int row = (half ? rowB : rowA) + r;
+            const int32_t v = half ? int32_t(int16_t(best[r] >> 16)) : int32_t(int16_t(best[r] & 0xFFFFu));
+            const int32_t c = half ? int32_t(bcol[r] >> 16) : int32_t(bcol[r] & 0xFFFFu);
+            if (row < m && v > lbest) {
+              lbest = v;
+              lrow = row + 1;
+              lcol = c;
+            }
+          }
+        }
+      } else if (pass == passes - 1) {
+        const int w = (m - 1) - pass * P2;  // row m within this pass
+        const int half = w >= P ? 1 : 0;
+        const int lr = (w - half * P) - t * R;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          if (r == lr) last_h = half ? int32_t(int16_t(H[r] >> 16)) : int32_t(int16_t(H[r] & 0xFFFFu));
+      }
+    }
+  }
+
+  // ---- results ---------------------------------------------------------
+  bool overflow = false;
+  if constexpr (CHECK) {
+    const int32_t lim = 32767 - A.max_score;
+    overflow = int32_t(int16_t(hmax & 0xFFFFu)) > lim || int32_t(int16_t(hmax >> 16)) > lim;
+  }
+  const bool goverflow = (__ballot_sync(0xffffffffu, overflow) & gm) != 0;
+  if constexpr (LOCAL) {
+    const uint64_t key = (uint64_t(uint32_t(lbest)) << 40) | (uint64_t(0xFFFFFu - uint32_t(lrow)) << 20) |
+                         uint64_t(0xFFFFFu - uint32_t(lcol));
+    const uint64_t gkey = group_max_rt(key, G);
+    if (have && t == 0) {
+      ResultDev &o = A.res[pid];
+      o.status = gbad ? TSQ_E_INVALID_RESIDUE : TSQ_OK;
+      const int32_t sc = int32_t(gkey >> 40);
+      o.score = sc;
+      o.a_end = sc > 0 ? int32_t(0xFFFFFu - uint32_t((gkey >> 20) & 0xFFFFFu)) : 0;
+      o.b_end = sc > 0 ? int32_t(0xFFFFFu - uint32_t(gkey & 0xFFFFFu)) : 0;
+      o.a_begin = o.b_begin = sc > 0 ? -1 : 0;
+      o.n_ident = o.n_cols = -1;
+      if (CHECK) A.overflow[pid] = goverflow ? 1 : 0;
+    }
+  } else {
+    int owner = 0;
+    if (m > 0) {
+      const int w = (m - 1) % P2;
+      owner = (w % P) / R;
+    }
+    const int32_t h = __shfl_sync(0xffffffffu, last_h, gw * G + owner);
+    if (have && t == 0) {
+      ResultDev &o = A.res[pid];
+      o.status = gbad ? TSQ_E_INVALID_RESIDUE : TSQ_OK;
+      o.a_begin = 0;
+      o.a_end = m;
+      o.b_begin = 0;
+      o.b_end = n;
+      o.score = (m == 0 || n == 0) ? ((m + n == 0) ? 0 : -(go + (m + n) * ge)) : h;
+      o.n_ident = o.n_cols = -1;
+      if (CHECK) A.overflow[pid] = goverflow ? 1 : 0;
+    }
+  }
+  __syncwarp();
+}
+
+template <bool LOCAL, bool CHECK>
+__global__ void __launch_bounds__(kThreads16) fill_i16_kernel(const FillArgs A) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  int8_t *s_mat = reinterpret_cast<int8_t *>(smem);
+  uint2 *s_prof = reinterpret_cast<uint2 *>(smem + kMatBytes);
+  uint8_t *s_rings = smem + kMatBytes + 2 * kLetters * kThreads16 * sizeof(uint2);
+  for (int k = threadIdx.x; k < kLetters * kLetters; k += blockDim.x) s_mat[k] = A.matrix[k];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int n_wtasks = A.n_wtasks_dev ? *A.n_wtasks_dev : A.n_wtasks;
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(A.counter, 1);
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= n_wtasks) break;
+    const int2 w = A.wtasks[idx];
+    const int G = w.y >> 16, count = w.y & 0xFFFF;
+    const int lg = G == 4 ? 2 : (G == 8 ? 3 : (G == 16 ? 4 : 5));
+    fill16_warp_task<LOCAL, CHECK>(A, s_mat, s_prof, s_rings, w.x, count, warp_id, 1 << lg, lg);
+  }
+}
+
+}  // namespace fill
+}  // namespace tsq

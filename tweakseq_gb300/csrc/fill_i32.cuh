@@ -35,108 +35,10 @@
 
 #include <cstdint>
 
-#include "tsq_internal.h"
+#include "fill_common.cuh"
 
 namespace tsq {
 namespace fill {
-
-constexpr int kThreads = 256;   // 8 warps per block
-constexpr int kMatBytes = 704;  // 26*26 int8 rounded up to a 64-byte multiple
-constexpr int kAhead = 4;       // step-loop unroll
-
-// Sign-extends byte K of w to 32 bits with one PRMT (selector bit 3 of each
-// nibble replicates the sign of the chosen byte).
-template <int K>
-__device__ __forceinline__ int32_t sbyte(uint32_t w) {
-  uint32_t d;
-  asm("prmt.b32 %0, %1, 0, %2;" : "=r"(d) : "r"(w), "n"(K | ((K | 8) << 4) | ((K | 8) << 8) | ((K | 8) << 12)));
-  return int32_t(d);
-}
-
-__device__ __forceinline__ int32_t sbyte_dyn(uint32_t w, int k) {
-  switch (k & 3) {
-    case 0: return sbyte<0>(w);
-    case 1: return sbyte<1>(w);
-    case 2: return sbyte<2>(w);
-    default: return sbyte<3>(w);
-  }
-}
-
-// Global-mode boundary value H(i,0) = H(0,i) = -(open + i*ext), H(0,0) = 0.
-__device__ __forceinline__ int32_t edge_h(int i, int32_t go, int32_t ge, bool local) {
-  return (local || i == 0) ? 0 : -(go + i * ge);
-}
-
-// Packed path counts for identity mode: (identical columns << 16) | columns.
-constexpr uint32_t kCol = 1u, kIdentCol = 0x10001u;
-
-template <int G>
-__device__ __forceinline__ unsigned group_mask(int lane) {
-  return G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((lane / G) * G));
-}
-
-template <int G, typename T>
-__device__ __forceinline__ T group_max(T v) {
-#pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1) {
-    T w = __shfl_xor_sync(0xffffffffu, v, o, G);
-    v = w > v ? w : v;
-  }
-  return v;
-}
-
-// Top-row entry carried from band to band: H and F, plus the path counts of
-// both in identity mode.
-template <int OUT>
-struct TopT {
-  using T = int2;
-};
-template <>
-struct TopT<kOutIdent> {
-  using T = int4;
-};
-
-// ---- staging rings --------------------------------------------------------
-// Each group keeps, in shared memory, a 64-column ring of its top row and a
-// 128-byte ring of b's residue codes.  They are filled by cp.async 32
-// columns ahead of use (one chunk in flight while the group sweeps the
-// previous one), so the step loop reads only shared memory.
-constexpr int kChunk = 32;       // columns per staged chunk
-constexpr int kTopRing = 64;     // top-row ring entries per group
-constexpr int kCodeRing = 128;   // code ring bytes per group
-constexpr int kSlotsPerBlock = kThreads / 32 * 8;  // 8 group slots per warp
-
-__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
-  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
-// Issues the copies of chunk k (columns [32k, 32k+32) of the top row and the
-// code bytes of columns [32k, 32k+32]) for one group; lane t of the group
-// takes copies t, t+G, ...  Nothing is copied past the pair's columns.
-template <int G, typename Top>
-__device__ __forceinline__ void stage_chunk(int k, int t, int nact, const Top *top_g, Top *top_ring,
-                                            const uint8_t *codes, int64_t boff, uint8_t *code_ring) {
-  constexpr int kPer = 16 / int(sizeof(Top));                  // entries per 16-byte copy
-  constexpr int kTopCopies = kChunk / kPer;
-  constexpr int kCopies = kTopCopies + 3;
-  const int c0 = kChunk * k;
-  if (c0 >= nact) return;
-  const int64_t a0 = (boff + c0) & ~int64_t(15);
-#pragma unroll
-  for (int q0 = 0; q0 < kCopies; q0 += G) {
-    const int q = q0 + t;
-    if (q < kTopCopies) {
-      const int e = c0 + q * kPer;
-      cp_async16(top_ring + (e & (kTopRing - 1)), top_g + e);
-    } else if (q < kCopies) {
-      const int64_t a = a0 + 16 * (q - kTopCopies);
-      cp_async16(code_ring + (a & (kCodeRing - 1)), codes + a);
-    }
-  }
-}
 
 // One warp task: the warp's 32/G groups each take one pair (or idle).
 template <int G, int R, bool LOCAL, int OUT>
@@ -158,8 +60,9 @@ __device__ __forceinline__ void fill_warp_task(const FillArgs &A, const int8_t *
   (void)GPW;
   // This group's staging rings.
   const int gslot = (threadIdx.x >> 5) * 8 + gw;
-  Top *top_ring = reinterpret_cast<Top *>(s_rings) + gslot * kTopRing;
-  uint8_t *code_ring = s_rings + kSlotsPerBlock * kTopRing * sizeof(Top) + gslot * kCodeRing;
+  constexpr int kTopStride = kTopRing * int(sizeof(Top)) + kRingPad;  // bytes
+  Top *top_ring = reinterpret_cast<Top *>(s_rings + gslot * kTopStride);
+  uint8_t *code_ring = s_rings + kSlotsPerBlock * kTopStride + gslot * (kCodeRing + kRingPad);
 
   {
     const bool have = gw < count;
@@ -518,11 +421,12 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<OUT>::value) fill_i32_kern
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int n_wtasks = A.n_wtasks_dev ? *A.n_wtasks_dev : A.n_wtasks;
   for (;;) {
     int idx = 0;
     if (lane == 0) idx = atomicAdd(A.counter, 1);
     idx = __shfl_sync(0xffffffffu, idx, 0);
-    if (idx >= A.n_wtasks) break;
+    if (idx >= n_wtasks) break;
     const int2 w = A.wtasks[idx];
     const int G = w.y >> 16, count = w.y & 0xFFFF;
     switch (G) {

@@ -66,6 +66,7 @@ struct FillArgs {
   const int32_t *tasks;  // pair ids, grouped by warp task
   const int2 *wtasks;
   int32_t n_wtasks;
+  const int32_t *n_wtasks_dev;  // when set, the warp-task count is read here (int32 re-run)
   int32_t *counter;      // work-queue head, zero before the launch
   const int8_t *matrix;  // 26*26 device copy of the scheme
   int32_t gap_open, gap_extend;
@@ -74,8 +75,15 @@ struct FillArgs {
   int32_t bnd_cols;      // entries per group row (max n over the launch, even)
   uint8_t *planes;       // TB planes (kOutTrace)
   const int64_t *plane_off;  // byte offset of each pair's planes
-  int32_t *overflow;     // int16: per pair flag, set when a lane saturated
+  int32_t *overflow;     // int16 CHECK: per pair, 1 when a lane came near 32767
+  int32_t max_score;     // largest substitution score of the scheme
 };
+
+// Compacts the pairs an int16 CHECK launch flagged into a warp-task list
+// for the int32 re-run (one pair per warp task, same lane width).
+cudaError_t launch_collect_overflow(const int32_t *checked, int32_t n_checked, const int32_t *overflow,
+                                    const int32_t *pair_g, int32_t *rerun_tasks, int2 *rerun_wtasks,
+                                    int32_t *rerun_count, cudaStream_t st);
 
 struct WalkArgs {
   const uint8_t *seqs;  // ASCII residues (for the emitted strings)
@@ -99,10 +107,12 @@ void build_lut(const Scheme &s, uint8_t lut[256]);
 
 // Kernel launchers (fill_kernels.cu, walk_kernel.cu, encode in batch.cu).
 // Returns the number of thread blocks a persistent launch of this shape uses.
-// A launch covers every lane width G of one row height R and lane type.
+// A launch covers every lane width G of one row height R and lane type
+// (i16: 0 int32, 1 int16x2, 2 int16x2 with overflow check).
 int fill_blocks(int R, int i16, int out_mode, bool local);
 size_t fill_smem_bytes(int R, int i16, int out_mode);
 int fill_threads();
+int fill_threads_for(int i16);
 size_t fill_bnd_entry_bytes(int i16, int out_mode);
 cudaError_t launch_fill(int R, int i16, int out_mode, bool local, const FillArgs &a, int blocks,
                         cudaStream_t st);
