@@ -172,6 +172,38 @@ int tsq_tune_run(const char *json_path, int32_t quick);
 /* Loads a tuned table written by tsq_tune_run (used when opts->autotune). */
 int tsq_tune_load(const char *json_path);
 
+/* ---- Allocation-free form --------------------------------------------------- */
+
+/* Result of one pair written to device memory (same fields as tsq_result,
+ * without strings). */
+typedef struct {
+  int32_t score;
+  int32_t a_begin, a_end, b_begin, b_end;
+  int32_t n_ident, n_cols;
+  int32_t status;
+} tsq_device_result;
+
+/* Score-only batch for callers that cannot allocate device memory (their
+ * memory is owned by another allocator, or allocation is not allowed on
+ * their path).  This entry point has no counterpart in the reference.  The
+ * caller passes device buffers it already owns -- residues d_seqs
+ * (seqs_len bytes), the pair table d_pairs (n entries) and the results d_out
+ * (n entries) -- and a CUDA stream (cudaStream_t, NULL for the legacy
+ * stream); the call enqueues its kernels and returns without waiting.  All
+ * intermediates live in one fixed 32 MiB device array inside the library
+ * (held by every GPU that loads it until the process exits); nothing is
+ * allocated.  Limits: seqs_len <= 8 MiB, n <= 1,048,576, max_len <= 2,048
+ * (larger values return TSQ_E_TOO_LARGE); a pair longer than max_len or
+ * outside the residue buffer gets status TSQ_E_TOO_LARGE / TSQ_E_INVALID_ARG
+ * in d_out.  p->output must be TSQ_OUT_SCORE; p->lane is ignored (int32).
+ * The first call on a device sets up the device address of the array and
+ * should come before any stream capture.  Calls share the array: two calls
+ * that overlap on the GPU race and corrupt each other's results. */
+int tsq_align_score_noalloc(const uint8_t *d_seqs, int64_t seqs_len,
+                            const tsq_pair_desc *d_pairs, int32_t n,
+                            int32_t max_len, const tsq_params *p,
+                            tsq_device_result *d_out, void *stream);
+
 /* ---- Device probe ---------------------------------------------------------- */
 
 /* Measured rate of the DP fill's DPX-class instructions (add-then-max and

@@ -123,6 +123,8 @@ _SIGS = {
     "tsq_tune_run": ([ctypes.c_char_p, ctypes.c_int32], ctypes.c_int),
     "tsq_tune_load": ([ctypes.c_char_p], ctypes.c_int),
     "tsq_probe_dpx": ([ctypes.c_int32, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    "tsq_align_score_noalloc": ([_VP, ctypes.c_int64, _VP, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(Params),
+                                 _VP, _VP], ctypes.c_int),
 }
 
 
