@@ -164,6 +164,54 @@ int tsq_batch_get_stats(const tsq_batch *b, tsq_batch_stats *st);
 int tsq_batch_stream(const tsq_batch *b, void **stream);
 void tsq_batch_destroy(tsq_batch *b);
 
+/* ---- Served form ----------------------------------------------------------- */
+
+/* A continuous-batching server on one GPU.  Requests (1 to millions of
+ * pairs, any parameters) are queued by tsq_server_submit from any thread; a
+ * scheduler thread groups waiting requests with equal parameters into
+ * ticks, admits a tick only while its device memory (residues, pair table,
+ * results, band-boundary rows and, for alignments, traceback planes) fits
+ * the HBM budget left by the ticks in flight, and runs up to `slots` ticks
+ * at once on separate streams.  Each request's results equal those of
+ * tsq_align_batch on that request alone. */
+typedef struct tsq_server tsq_server;
+
+typedef struct {
+  int32_t device;           /* CUDA ordinal; -1 = current device */
+  int32_t slots;            /* ticks in flight at once (0 = 4) */
+  int64_t hbm_budget_bytes; /* admission budget (0 = half the free HBM at creation) */
+  int64_t max_tick_cells;   /* DP cells per tick before it closes (0 = 4e10) */
+  int32_t autotune;         /* 1 = plan ticks with the tuned table */
+  int32_t reserved;
+} tsq_server_opts;
+
+typedef struct {
+  int64_t submitted, completed, rejected, cancelled;
+  int64_t ticks;                /* launches planned so far */
+  int64_t cells_completed;      /* DP cells of completed requests */
+  int64_t peak_reserved_bytes;  /* largest HBM reservation of ticks in flight */
+  int64_t admission_waits;      /* times the oldest request waited for memory */
+  double p50_ms, p99_ms, max_ms; /* submit-to-completion latency */
+  double span_s;                /* first submit to last completion */
+} tsq_server_stats;
+
+int tsq_server_create(const tsq_server_opts *opts, tsq_server **out);
+/* Queues a request (the inputs are copied); TSQ_E_REJECTED if it could never
+ * fit the budget, TSQ_E_INVALID_ARG for a bad pair table. */
+int tsq_server_submit(tsq_server *s, const uint8_t *seqs, int64_t seqs_len,
+                      const tsq_pair_desc *pairs, int64_t n, const tsq_params *p,
+                      uint64_t *request_id);
+/* Waits up to wait_ms (0: no wait, <0: forever) for a request.  When it is
+ * done, copies its n results to out (strings owned by the caller, release
+ * with tsq_results_free), forgets the request and returns its status;
+ * otherwise TSQ_E_PENDING.  TSQ_E_CANCELLED / TSQ_E_NOT_FOUND as named. */
+int tsq_server_poll(tsq_server *s, uint64_t id, int32_t wait_ms, tsq_result *out, int64_t n);
+/* Cancels a request that has not reached the device (TSQ_E_PENDING if it has). */
+int tsq_server_cancel(tsq_server *s, uint64_t id);
+int tsq_server_get_stats(tsq_server *s, tsq_server_stats *st);
+/* Finishes the ticks in flight, cancels waiting requests, frees everything. */
+int tsq_server_destroy(tsq_server *s);
+
 /* ---- Autotuner ------------------------------------------------------------ */
 
 /* Measures the compiled kernel shapes on the current device over seeded

@@ -80,6 +80,19 @@ class BatchOpts(ctypes.Structure):
                 ("reserved", ctypes.c_int32)]
 
 
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("slots", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64),
+                ("max_tick_cells", ctypes.c_int64), ("autotune", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64), ("rejected", ctypes.c_int64),
+                ("cancelled", ctypes.c_int64), ("ticks", ctypes.c_int64), ("cells_completed", ctypes.c_int64),
+                ("peak_reserved_bytes", ctypes.c_int64), ("admission_waits", ctypes.c_int64),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
+                ("span_s", ctypes.c_double)]
+
+
 class BatchStats(ctypes.Structure):
     _fields_ = [
         ("cells", ctypes.c_int64),
@@ -120,6 +133,13 @@ _SIGS = {
     "tsq_batch_get_stats": ([_VP, ctypes.POINTER(BatchStats)], ctypes.c_int),
     "tsq_batch_stream": ([_VP, ctypes.POINTER(_VP)], ctypes.c_int),
     "tsq_batch_destroy": ([_VP], None),
+    "tsq_server_create": ([ctypes.POINTER(ServerOpts), ctypes.POINTER(_VP)], ctypes.c_int),
+    "tsq_server_submit": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.POINTER(Params),
+                           ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+    "tsq_server_poll": ([_VP, ctypes.c_uint64, ctypes.c_int32, _VP, ctypes.c_int64], ctypes.c_int),
+    "tsq_server_cancel": ([_VP, ctypes.c_uint64], ctypes.c_int),
+    "tsq_server_get_stats": ([_VP, ctypes.POINTER(ServerStats)], ctypes.c_int),
+    "tsq_server_destroy": ([_VP], ctypes.c_int),
     "tsq_tune_run": ([ctypes.c_char_p, ctypes.c_int32], ctypes.c_int),
     "tsq_tune_load": ([ctypes.c_char_p], ctypes.c_int),
     "tsq_probe_dpx": ([ctypes.c_int32, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),

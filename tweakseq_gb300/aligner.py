@@ -239,3 +239,72 @@ def probe_dpx(packed: bool = False) -> float:
     v = ctypes.c_double()
     N.check(N.lib().tsq_probe_dpx(int(packed), ctypes.byref(v)), "tsq_probe_dpx")
     return v.value
+
+
+class Server:
+    """Continuous-batching server (tsq_server_*): submit requests of any
+    size from any thread, poll their results; the library's scheduler thread
+    groups, admits (by HBM budget) and overlaps them on the GPU."""
+
+    def __init__(self, slots=4, hbm_budget_bytes=0, max_tick_cells=0, autotune=False, device=-1):
+        o = N.ServerOpts()
+        o.device, o.slots, o.hbm_budget_bytes, o.max_tick_cells = device, slots, hbm_budget_bytes, max_tick_cells
+        o.autotune = int(bool(autotune))
+        h = ctypes.c_void_p()
+        N.check(N.lib().tsq_server_create(ctypes.byref(o), ctypes.byref(h)), "tsq_server_create")
+        self._h = h
+        self._meta = {}
+
+    def submit(self, pairs, matrix="blosum62", gap_open=11, gap_extend=1, mode="global", output="alignment",
+               lane="auto", custom=None) -> int:
+        seqs, tab = _as_inputs(pairs)
+        p, keep = N.make_params(matrix, gap_open, gap_extend, mode, output, lane, custom)
+        rid = ctypes.c_uint64()
+        rc = N.lib().tsq_server_submit(self._h, seqs.ctypes.data if len(seqs) else None, len(seqs),
+                                       tab.ctypes.data if len(tab) else None, len(tab), ctypes.byref(p),
+                                       ctypes.byref(rid))
+        del keep
+        N.check(rc, "tsq_server_submit")
+        self._meta[rid.value] = (len(tab), output)
+        return rid.value
+
+    def poll(self, rid: int, wait_ms: int = -1, check=True):
+        """Returns the request's BatchResult, or None while it is pending."""
+        n, output = self._meta[rid]
+        raw = np.zeros(n, dtype=N.RESULT_DTYPE)
+        rc = N.lib().tsq_server_poll(self._h, rid, int(wait_ms), raw.ctypes.data if n else None, n)
+        if rc == N.E_PENDING:
+            return None
+        if rc not in (N.TSQ_OK, N.E_INVALID_RESIDUE):
+            self._meta.pop(rid, None)
+            N.check(rc, "tsq_server_poll")
+        self._meta.pop(rid, None)
+        res = _collect(raw, output in ("alignment", 2))
+        if check and rc != N.TSQ_OK:
+            N.check(rc, "tsq_server_poll")
+        return res
+
+    def cancel(self, rid: int) -> int:
+        return N.lib().tsq_server_cancel(self._h, rid)
+
+    def stats(self) -> dict:
+        st = N.ServerStats()
+        N.check(N.lib().tsq_server_get_stats(self._h, ctypes.byref(st)), "tsq_server_get_stats")
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().tsq_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

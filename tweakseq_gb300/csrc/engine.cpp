@@ -112,6 +112,7 @@ Shape ShapeChooser::pick(int m, int n, int rows_per_lane) const {
 }  // namespace tsq
 
 tsq_batch::~tsq_batch() {
+  if (ev_fetch) cudaEventDestroy(ev_fetch);
   if (gexec) cudaGraphExecDestroy(gexec);
   if (graph) cudaGraphDestroy(graph);
   for (auto &e : ev)
@@ -542,19 +543,32 @@ int batch_sync(tsq_batch *b) {
   return TSQ_OK;
 }
 
-int batch_results(tsq_batch *b, tsq_result *out) {
-  if (!b || (b->n > 0 && !out)) return TSQ_E_INVALID_ARG;
-  if (!b->has_run) return TSQ_E_INVALID_ARG;
+int batch_fetch_async(tsq_batch *b) {
+  if (!b || !b->has_run) return TSQ_E_INVALID_ARG;
   cudaStream_t st = b->stream;
   if (b->n > 0)
     TSQ_TRY(cudaMemcpyAsync(b->res_h.p, b->res.p, sizeof(ResultDev) * size_t(b->n), cudaMemcpyDeviceToHost, st));
   if (b->out_mode == kOutTrace && b->aln_bytes > 0)
     TSQ_TRY(cudaMemcpyAsync(b->aln_h.p, b->aln.p, size_t(b->aln_bytes), cudaMemcpyDeviceToHost, st));
-  TSQ_TRY(cudaStreamSynchronize(st));
+  if (!b->ev_fetch) TSQ_TRY(cudaEventCreateWithFlags(&b->ev_fetch, cudaEventDisableTiming));
+  TSQ_TRY(cudaEventRecord(b->ev_fetch, st));
+  return TSQ_OK;
+}
+
+int batch_fetch_query(tsq_batch *b) {
+  const cudaError_t e = cudaEventQuery(b->ev_fetch);
+  if (e == cudaSuccess) return TSQ_OK;
+  if (e == cudaErrorNotReady) return TSQ_E_PENDING;
+  return cuda_status(e);
+}
+
+int batch_collect(tsq_batch *b, int64_t begin, int64_t count, tsq_result *out) {
+  if (!b || begin < 0 || count < 0 || begin + count > b->n || (count > 0 && !out)) return TSQ_E_INVALID_ARG;
   const ResultDev *r = b->res_h.as<ResultDev>();
   int rc = TSQ_OK;
-  for (int64_t k = 0; k < b->n; ++k) {
-    tsq_result &o = out[k];
+  for (int64_t q = 0; q < count; ++q) {
+    const int64_t k = begin + q;
+    tsq_result &o = out[q];
     const ResultDev &d = r[k];
     o.score = d.score;
     o.a_begin = d.a_begin;
@@ -566,7 +580,8 @@ int batch_results(tsq_batch *b, tsq_result *out) {
     o.status = d.status;
     o.aln_a = o.aln_b = nullptr;
     if (d.status != TSQ_OK) {
-      rc = TSQ_E_INVALID_RESIDUE;
+      // A residue error is the caller's; anything else is the library's.
+      if (rc == TSQ_OK || d.status != TSQ_E_INVALID_RESIDUE) rc = d.status;
       continue;
     }
     if (b->out_mode == kOutTrace) {
@@ -590,6 +605,23 @@ int batch_results(tsq_batch *b, tsq_result *out) {
     }
   }
   return rc;
+}
+
+int batch_results(tsq_batch *b, tsq_result *out) {
+  if (!b || (b->n > 0 && !out)) return TSQ_E_INVALID_ARG;
+  int rc = batch_fetch_async(b);
+  if (rc) return rc;
+  TSQ_TRY(cudaStreamSynchronize(b->stream));
+  return batch_collect(b, 0, b->n, out);
+}
+
+int64_t batch_device_bytes(const tsq_batch *b) {
+  const tsq::DevBuf *bufs[] = {&b->seqs, &b->codes, &b->pairs, &b->tasks, &b->wtasks, &b->res, &b->bnd,
+                               &b->planes, &b->plane_off, &b->aln, &b->aln_off, &b->shape_g, &b->shape_r,
+                               &b->counters, &b->lut, &b->matrix, &b->overflow, &b->rerun_tasks, &b->rerun_wtasks};
+  int64_t total = 0;
+  for (const tsq::DevBuf *d : bufs) total += int64_t(d->cap);
+  return total;
 }
 
 }  // namespace tsq

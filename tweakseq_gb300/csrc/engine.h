@@ -79,6 +79,7 @@ struct tsq_batch {
   // when captured); ev[4..5]: around a graph launch.
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   bool capturing = false;
+  cudaEvent_t ev_fetch = nullptr;  // results copied to the pinned host buffers
   tsq::Scheme scheme{};
   tsq_params params{};
   int out_mode = tsq::kOutScore;
@@ -113,5 +114,10 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
 int batch_run_async(tsq_batch *b);
 int batch_sync(tsq_batch *b);
 int batch_results(tsq_batch *b, tsq_result *out);
+// Asynchronous read-back: enqueue the copies, poll, then convert a range.
+int batch_fetch_async(tsq_batch *b);
+int batch_fetch_query(tsq_batch *b);  // TSQ_OK when the copies landed, TSQ_E_PENDING before
+int batch_collect(tsq_batch *b, int64_t begin, int64_t count, tsq_result *out);
+int64_t batch_device_bytes(const tsq_batch *b);
 int cuda_status(cudaError_t e);
 }  // namespace tsq
