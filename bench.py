@@ -41,7 +41,7 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = ("uneven_pairs_100k: 100,000 protein pairs, lengths log-normal (median 350, sigma 0.5, clipped 50-2000), "
             "partner 30-90% identity with 5% indels, seed 2; BLOSUM62, gap 11/1, global, score only")
-METRIC = "GCUPS (batched, 100k uneven protein pairs, score-only, bit-exact)"
+METRIC = "GCUPS (batched, 100k uneven protein pairs, score-only, bit-exact); served p50/p99 in 'serving'"
 CPU_SAMPLE_PAIRS = 20000
 
 
@@ -56,6 +56,8 @@ def parse_args():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", type=int, default=0, metavar="PAIRS",
                     help="profiling case: only the batched leg over the first PAIRS pairs, no graph")
+    ap.add_argument("--serve-requests", type=int, default=120, help="requests in the serving leg (0 = skip)")
+    ap.add_argument("--serve-only", action="store_true", help="run only the serving leg and print it")
     return ap.parse_args()
 
 
@@ -292,6 +294,8 @@ def run_ours(args):
         bitexact = {"pairs_checked": int(len(idx)), "mismatches": mism}
         cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
+    serving = serve_leg(args.serve_requests) if args.serve_requests > 0 else None
+
     clocks = clk.summary()
     line = {
         "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
@@ -311,10 +315,85 @@ def run_ours(args):
         "bitexact": bitexact,
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def serve_leg(n_requests=120, loads=(0.25, 0.5, 0.9), seed=5, plain_pairs=600):
+    """Served form on the serving workload: Poisson arrivals of requests of
+    1-2,000 pairs (log-uniform), protein (BLOSUM62 11/1) or DNA (+2/-3, 5/2),
+    lengths 50-5,000 (log-uniform), traceback on half of the requests.
+
+    Capacity is measured closed-loop (every request submitted at once); the
+    offered loads are fractions of it.  Latency is submit-to-completion of
+    each request (server statistics).  The plain per-pair path runs the
+    same pairs one tsq_align_pair call at a time on a sample."""
+    from tweakseq_gb300 import aligner as A
+    from tweakseq_gb300 import workloads as W
+
+    reqs = W.serving_stream(n_requests, 1.0, seed=seed)
+
+    def kw(r):
+        base = dict(matrix="dna", gap_open=5, gap_extend=2) if r.pairs.matrix == W.DNA else {}
+        return dict(base, output="alignment" if r.traceback else "score")
+
+    cells = np.array([r.pairs.cells for r in reqs], dtype=np.float64)
+    total = float(cells.sum())
+    # Warm the server path (planning, first launches) before measuring.
+    with A.Server(slots=4) as srv:
+        for r in reqs[:4]:
+            srv.poll(srv.submit(r.pairs, **kw(r)))
+    with A.Server(slots=4) as srv:
+        t0 = time.perf_counter()
+        ids = [srv.submit(r.pairs, **kw(r)) for r in reqs]
+        for rid in ids:
+            srv.poll(rid)
+        closed_s = time.perf_counter() - t0
+        st = srv.stats()
+    capacity = total / closed_s  # cells per second
+    out = {"workload": f"{n_requests} requests, {int(sum(len(r.pairs) for r in reqs))} pairs, {total:.3e} cells, "
+                       "1-2000 pairs per request (log-uniform), protein or DNA, lengths 50-5000, traceback on half",
+           "capacity_gcups": capacity / 1e9, "closed_loop": {"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                                                              "ticks": st["ticks"]}, "loads": []}
+    rng = np.random.default_rng(seed + 1)
+    for load in loads:
+        lam = load * capacity / float(cells.mean())  # requests per second
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, size=len(reqs)))
+        with A.Server(slots=4) as srv:
+            t0 = time.perf_counter()
+            ids = []
+            for r, t_arr in zip(reqs, arrivals):
+                delay = t0 + t_arr - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                ids.append(srv.submit(r.pairs, **kw(r)))
+            for rid in ids:
+                srv.poll(rid)
+            st = srv.stats()
+        out["loads"].append({"offered": load, "offered_gcups": load * capacity / 1e9,
+                             "achieved_gcups": total / st["span_s"] / 1e9, "p50_ms": st["p50_ms"],
+                             "p99_ms": st["p99_ms"], "max_ms": st["max_ms"], "ticks": st["ticks"],
+                             "peak_hbm_gb": st["peak_reserved_bytes"] / 1e9})
+    # Plain per-pair path on a sample of the same pairs (score and
+    # traceback as each request asks).
+    sample_cells, t_plain, done = 0, 0.0, 0
+    for r in reqs:
+        if done >= plain_pairs:
+            break
+        for k in range(min(len(r.pairs), plain_pairs - done)):
+            a, b = r.pairs.pair(k)
+            t0 = time.perf_counter()
+            A.align_pair(a, b, **kw(r))
+            t_plain += time.perf_counter() - t0
+            sample_cells += len(a) * len(b)
+            done += 1
+    out["plain_gcups"] = sample_cells / t_plain / 1e9
+    out["plain_pairs_sampled"] = done
+    out["served_over_plain"] = out["capacity_gcups"] / out["plain_gcups"]
+    return out
 
 
 def run_profile(args):
@@ -342,6 +421,11 @@ def main():
     args = parse_args()
     if args.profile:
         run_profile(args)
+        return
+    if args.serve_only:
+        from tweakseq_gb300 import build as B
+        B.build()
+        print(json.dumps({"serving": serve_leg(args.serve_requests)}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

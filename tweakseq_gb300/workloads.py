@@ -155,32 +155,37 @@ def uneven_pairs(n_pairs: int = 100_000, median: float = 350.0, sigma: float = 0
 
 
 def _mutate_dna(rng, ref: np.ndarray, sub: float, indel: float, mean_len: float) -> np.ndarray:
+    """Substitutions (to one of the three other bases) at rate sub, and indel
+    events at rate indel per position with geometric lengths (mean
+    mean_len), half deletions and half insertions of random bases."""
     L = len(ref)
     q = ref.copy()
     m = rng.random(L) < sub
-    # Substitute with one of the three other bases.
     shift = rng.integers(1, 4, size=int(m.sum()))
     idx = np.searchsorted(DNA_LETTERS, q[m])
     q[m] = DNA_LETTERS[(idx + shift) % 4]
-    keep = np.ones(L, dtype=np.int64)
     events = np.flatnonzero(rng.random(L) < indel)
-    pieces = []
-    ins_after = {}
-    for p in events:
-        ln = int(rng.geometric(1.0 / mean_len))
-        if rng.random() < 0.5:
-            keep[p:p + ln] = 0
-        else:
-            ins_after[int(p)] = DNA_LETTERS[rng.integers(0, 4, size=ln)]
-    if not ins_after:
-        return np.repeat(q, keep)
-    last = 0
-    for p in sorted(ins_after):
-        pieces.append(np.repeat(q[last:p + 1], keep[last:p + 1]))
-        pieces.append(ins_after[p])
-        last = p + 1
-    pieces.append(np.repeat(q[last:], keep[last:]))
-    return np.concatenate(pieces)
+    lens = rng.geometric(1.0 / mean_len, size=len(events))
+    is_del = rng.random(len(events)) < 0.5
+    # Deletions: mark [p, p + len) through a difference array.
+    diff = np.zeros(L + 1, dtype=np.int64)
+    np.add.at(diff, events[is_del], 1)
+    np.add.at(diff, np.minimum(events[is_del] + lens[is_del], L), -1)
+    keep = (np.cumsum(diff[:L]) == 0).astype(np.int64)
+    # Insertions: repeat the base at p 1 + len times, then randomise the copies.
+    counts = keep.copy()
+    ins_at = events[~is_del]
+    ins_len = lens[~is_del]
+    ok = keep[ins_at] > 0
+    np.add.at(counts, ins_at[ok], ins_len[ok])
+    out = np.repeat(q, counts)
+    ends = np.cumsum(counts)
+    starts = ends - counts
+    fresh = np.zeros(len(out), dtype=bool)
+    for p, ln in zip(ins_at[ok], ins_len[ok]):
+        fresh[starts[p] + 1:starts[p] + 1 + ln] = True
+    out[fresh] = DNA_LETTERS[rng.integers(0, 4, size=int(fresh.sum()))]
+    return out
 
 
 def long_dna_pairs(n_pairs: int = 1000, lo: int = 10_000, hi: int = 50_000, sub: float = 0.10, indel: float = 0.02,
