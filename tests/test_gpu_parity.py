@@ -265,3 +265,32 @@ def test_mixed_lane_types_one_batch():
         got = A.align_batch(ps, gap_open=20, gap_extend=60, mode="local" if local else "global", output="score")
         want = O.batch(ps.seqs, ps.a_off, ps.a_len, ps.b_off, ps.b_len, O.BLOSUM62, 20, 60, local, O.MODE_SCORE)
         assert_same(got, want, score_fields(local), "mixed")
+
+
+@pytest.mark.parametrize("local", [False, True])
+def test_long_pairs_on_the_cta_fill_all_outputs(local):
+    """Pairs long enough for the CTA fill (bands striped over 8 warps):
+    79, 12 and 3 bands (fewer bands than warps), long rows and long
+    columns, score / identity / alignment, against the oracle."""
+    rng = np.random.default_rng(17 + local)
+    seqs, pairs = [], []
+    for m, n in ((20000, 3000), (3000, 20000), (2900, 2700), (700, 9000)):
+        a = W.DNA_LETTERS[rng.integers(0, 4, m)]
+        b = W._mutate_dna(rng, a, 0.1, 0.02, 3.0)[:n] if n <= m else W.DNA_LETTERS[rng.integers(0, 4, n)]
+        if n > m:
+            b[: m // 2] = a[: m // 2]  # related prefix so the alignment is not trivial
+        seqs += [a.tobytes(), b.tobytes()]
+        pairs.append((len(seqs) - 2, len(seqs) - 1))
+    ps = W._pairset_from_lists(seqs, pairs, matrix=W.DNA, gap_open=5, gap_extend=2)
+    got = gpu_batch(ps, local, "score")
+    assert_same(got, oracle_batch(ps, local, O.MODE_SCORE), score_fields(local), "cta score")
+    got = gpu_batch(ps, local, "identity")
+    assert_same(got, oracle_batch(ps, local, O.MODE_IDENT), ident_fields(local), "cta identity")
+    got = gpu_batch(ps, local, "alignment")
+    want, sa, sb = oracle_batch(ps, local, O.MODE_ALIGN, strings=True)
+    assert_same(got, want, FIELDS, "cta alignment")
+    assert got.aln_a == sa and got.aln_b == sb
+    # The plain form of a long pair takes the same path.
+    a, b = ps.pair(2)
+    r = A.align_pair(a, b, matrix="dna", gap_open=5, gap_extend=2, mode="local" if local else "global")
+    assert (r.score, r.aln_a, r.aln_b) == (int(want["score"][2]), sa[2], sb[2])

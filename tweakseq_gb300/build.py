@@ -19,6 +19,8 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libtsq_gb300.so")
+CLI_SRC = os.path.join(PKG, "cli", "tsq_align.cpp")
+CLI = os.path.join(LIBDIR, "tsq_align")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "-I", os.path.join(ROOT, "include")]
@@ -40,10 +42,22 @@ def _deps() -> list[str]:
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CLI):
         return False
-    t = os.path.getmtime(LIB)
-    return all(os.path.getmtime(d) <= t for d in _deps())
+    t = min(os.path.getmtime(LIB), os.path.getmtime(CLI))
+    return all(os.path.getmtime(d) <= t for d in _deps() + [CLI_SRC])
+
+
+def build_cli() -> str:
+    """The tsq_align command-line tool (host C++ linked to the library)."""
+    cxx = shutil.which("g++") or "g++"
+    tmp = CLI + ".tmp"
+    r = subprocess.run([cxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), CLI_SRC, "-o", tmp,
+                        "-L", LIBDIR, "-ltsq_gb300", "-Wl,-rpath,$ORIGIN"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"tsq_align build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, CLI)
+    return CLI
 
 
 def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> str:
@@ -73,6 +87,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli()
     return LIB
 
 

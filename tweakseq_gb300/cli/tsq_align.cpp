@@ -1,0 +1,239 @@
+// tsq_align -- command-line front end of the GB300 alignment library, a
+// drop-in for the external aligner behind the editor's AlignmentTool seam.
+//
+// The editor writes the sequences to align as FASTA and runs
+// `<exec> <args>` built by AlignmentTool::makeCommand, reading the gapped
+// result back as FASTA (tweakseq/Core/AlignmentTool.h:36-71,
+// tweakseq/UI/SeqEditMainWin.cpp:1616-1663, Project::readNewAlignment in
+// tweakseq/Core/Project.cpp:908-1032).  This program accepts the same shapes
+// of command line as the tools the editor knows (MUSCLE-style `-in F -out
+// F`, ClustalO-style `-i F -o F`, or output on stdout as MAFFT does) and:
+//
+//   two sequences  -> their pairwise alignment as gapped FASTA, same labels
+//                     and header lines, 80 residues per line (the editor's
+//                     own FASTA writer wraps at 80, FASTAFile.cpp:149-171);
+//   --all-vs-all   -> every unordered pair, one TSV line per pair: labels,
+//                     score, identical columns, columns, percent identity
+//                     (the distance input of a guide tree).
+//
+// FASTA is read as the editor reads it (FASTAFile.cpp:71-147): a record
+// starts at '>' or ';', its label is the header text up to the first space,
+// further ';' lines right after a header are comments, sequence lines are
+// concatenated.  Gap characters already in the input ('-', '.') are dropped
+// and residues upper-cased, as the external aligners do with editor output.
+#include <cctype>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/tweakseq_gb300.h"
+
+namespace {
+
+struct Record {
+  std::string header;  // the whole header line, '>' included
+  std::string label;
+  std::string residues;
+};
+
+bool read_fasta(std::istream &in, std::vector<Record> &out, std::string &err) {
+  std::string line;
+  enum { kSeek, kComment, kSequence } state = kSeek;
+  while (std::getline(in, line)) {
+    // Trim like QString::trimmed.
+    size_t a = 0, b = line.size();
+    while (a < b && std::isspace(static_cast<unsigned char>(line[a]))) ++a;
+    while (b > a && std::isspace(static_cast<unsigned char>(line[b - 1]))) --b;
+    line = line.substr(a, b - a);
+    if (line.empty()) continue;
+    const char c = line[0];
+    if (c == '>' || c == ';') {
+      if (state == kComment && c == ';') continue;  // further comment lines
+      Record r;
+      r.header = line;
+      const size_t sp = line.find(' ', 1);
+      r.label = sp == std::string::npos ? line.substr(1) : line.substr(1, sp - 1);
+      out.push_back(r);
+      state = kComment;
+      continue;
+    }
+    if (state == kSeek) continue;
+    for (char ch : line) {
+      if (ch == '-' || ch == '.' || std::isspace(static_cast<unsigned char>(ch))) continue;
+      out.back().residues.push_back(char(std::toupper(static_cast<unsigned char>(ch))));
+    }
+    state = kSequence;
+  }
+  if (out.empty()) {
+    err = "no FASTA records";
+    return false;
+  }
+  return true;
+}
+
+void write_wrapped(std::ostream &o, const std::string &header, const std::string &s) {
+  o << header << '\n';
+  for (size_t k = 0; k < s.size(); k += 80) o << s.substr(k, 80) << '\n';
+}
+
+void usage() {
+  std::fprintf(stderr,
+               "usage: tsq_align [-in|-i FILE] [-out|-o FILE] [--local] [--dna | --matrix blosum62|dna]\n"
+               "                 [--gap-open N] [--gap-extend N] [--all-vs-all]\n"
+               "  Two sequences: gapped FASTA of their alignment (stdout when no output file).\n"
+               "  --all-vs-all: TSV of every pair (label_a, label_b, score, n_ident, n_cols, identity %%).\n");
+}
+
+const char *status_name(int rc) {
+  switch (rc) {
+    case TSQ_E_INVALID_ARG: return "invalid argument";
+    case TSQ_E_INVALID_RESIDUE: return "invalid residue for the scoring matrix";
+    case TSQ_E_NOMEM: return "out of memory";
+    case TSQ_E_CUDA: return "CUDA error (no usable GPU?)";
+    case TSQ_E_TOO_LARGE: return "input too large";
+    default: return "error";
+  }
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  std::string fin, fout;
+  tsq_params p{};
+  p.matrix = TSQ_MATRIX_BLOSUM62;
+  p.gap_open = 11;
+  p.gap_extend = 1;
+  p.mode = TSQ_GLOBAL;
+  p.output = TSQ_OUT_ALIGNMENT;
+  p.lane = TSQ_LANE_AUTO;
+  bool all_vs_all = false, gaps_set = false;
+  for (int k = 1; k < argc; ++k) {
+    const std::string a = argv[k];
+    auto next = [&](const char *what) -> std::string {
+      if (k + 1 >= argc) {
+        std::fprintf(stderr, "tsq_align: %s needs a value\n", what);
+        std::exit(2);
+      }
+      return argv[++k];
+    };
+    if (a == "-in" || a == "-i" || a == "--in") fin = next("-in");
+    else if (a == "-out" || a == "-o" || a == "--out") fout = next("-out");
+    else if (a == "--local") p.mode = TSQ_LOCAL;
+    else if (a == "--dna") p.matrix = TSQ_MATRIX_DNA;
+    else if (a == "--matrix") {
+      const std::string m = next("--matrix");
+      if (m == "blosum62") p.matrix = TSQ_MATRIX_BLOSUM62;
+      else if (m == "dna") p.matrix = TSQ_MATRIX_DNA;
+      else {
+        std::fprintf(stderr, "tsq_align: unknown matrix %s\n", m.c_str());
+        return 2;
+      }
+    } else if (a == "--gap-open") {
+      p.gap_open = std::atoi(next("--gap-open").c_str());
+      gaps_set = true;
+    } else if (a == "--gap-extend") {
+      p.gap_extend = std::atoi(next("--gap-extend").c_str());
+      gaps_set = true;
+    } else if (a == "--all-vs-all") all_vs_all = true;
+    else if (a == "-h" || a == "--help") {
+      usage();
+      return 0;
+    } else if (fin.empty() && a[0] != '-') fin = a;  // MAFFT style: input file as the last argument
+    else {
+      std::fprintf(stderr, "tsq_align: unknown argument %s\n", a.c_str());
+      usage();
+      return 2;
+    }
+  }
+  if (p.matrix == TSQ_MATRIX_DNA && !gaps_set) {
+    p.gap_open = 5;
+    p.gap_extend = 2;
+  }
+  std::vector<Record> recs;
+  std::string err;
+  {
+    std::ifstream f;
+    std::istream *in = &std::cin;
+    if (!fin.empty()) {
+      f.open(fin);
+      if (!f) {
+        std::fprintf(stderr, "tsq_align: cannot open %s\n", fin.c_str());
+        return 1;
+      }
+      in = &f;
+    }
+    if (!read_fasta(*in, recs, err)) {
+      std::fprintf(stderr, "tsq_align: %s\n", err.c_str());
+      return 1;
+    }
+  }
+  std::ofstream fo;
+  std::ostream *out = &std::cout;
+  if (!fout.empty()) {
+    fo.open(fout);
+    if (!fo) {
+      std::fprintf(stderr, "tsq_align: cannot write %s\n", fout.c_str());
+      return 1;
+    }
+    out = &fo;
+  }
+
+  if (!all_vs_all) {
+    if (recs.size() != 2) {
+      std::fprintf(stderr, "tsq_align: pairwise alignment needs exactly 2 sequences (got %zu); "
+                           "use --all-vs-all for more\n",
+                   recs.size());
+      return 1;
+    }
+    tsq_result r;
+    const std::string &a = recs[0].residues, &b = recs[1].residues;
+    const int rc = tsq_align_pair(reinterpret_cast<const uint8_t *>(a.data()), int32_t(a.size()),
+                                  reinterpret_cast<const uint8_t *>(b.data()), int32_t(b.size()), &p, &r);
+    if (rc != TSQ_OK) {
+      std::fprintf(stderr, "tsq_align: %s\n", status_name(rc));
+      return 1;
+    }
+    write_wrapped(*out, recs[0].header, r.aln_a);
+    write_wrapped(*out, recs[1].header, r.aln_b);
+    tsq_result_free(&r);
+    return 0;
+  }
+
+  // All-vs-all: one residue buffer, every unordered pair, identity output.
+  std::string buf;
+  std::vector<int64_t> off;
+  for (const Record &r : recs) {
+    off.push_back(int64_t(buf.size()));
+    buf += r.residues;
+  }
+  std::vector<tsq_pair_desc> pairs;
+  for (size_t x = 0; x < recs.size(); ++x)
+    for (size_t y = x + 1; y < recs.size(); ++y)
+      pairs.push_back(tsq_pair_desc{off[x], off[y], int32_t(recs[x].residues.size()),
+                                    int32_t(recs[y].residues.size())});
+  p.output = TSQ_OUT_IDENTITY;
+  std::vector<tsq_result> res(pairs.size());
+  tsq_batch_opts o{-1, 0, 0, 0};
+  const int rc = tsq_align_batch(reinterpret_cast<const uint8_t *>(buf.data()), int64_t(buf.size()), pairs.data(),
+                                 int64_t(pairs.size()), &p, &o, res.data());
+  if (rc != TSQ_OK) {
+    std::fprintf(stderr, "tsq_align: %s\n", status_name(rc));
+    return 1;
+  }
+  *out << "label_a\tlabel_b\tscore\tn_ident\tn_cols\tidentity_pct\n";
+  size_t k = 0;
+  for (size_t x = 0; x < recs.size(); ++x)
+    for (size_t y = x + 1; y < recs.size(); ++y, ++k) {
+      const tsq_result &r = res[k];
+      char pct[32];
+      std::snprintf(pct, sizeof(pct), "%.2f", r.n_cols > 0 ? 100.0 * r.n_ident / r.n_cols : 0.0);
+      *out << recs[x].label << '\t' << recs[y].label << '\t' << r.score << '\t' << r.n_ident << '\t' << r.n_cols
+           << '\t' << pct << '\n';
+    }
+  return 0;
+}

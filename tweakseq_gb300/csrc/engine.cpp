@@ -113,6 +113,9 @@ Shape ShapeChooser::pick(int m, int n, int rows_per_lane) const {
 
 tsq_batch::~tsq_batch() {
   if (ev_fetch) cudaEventDestroy(ev_fetch);
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  if (ev_join) cudaEventDestroy(ev_join);
+  if (side) cudaStreamDestroy(side);
   if (gexec) cudaGraphExecDestroy(gexec);
   if (graph) cudaGraphDestroy(graph);
   for (auto &e : ev)
@@ -155,9 +158,14 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   if (b->stream && b->device != dev) {
     cudaStreamDestroy(b->stream);
     b->stream = nullptr;
+    if (b->side) cudaStreamDestroy(b->side);
+    b->side = nullptr;
   }
   b->device = dev;
   if (!b->stream) TSQ_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  if (!b->side) TSQ_TRY(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+  if (!b->ev_fork) TSQ_TRY(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+  if (!b->ev_join) TSQ_TRY(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
   for (auto &e : b->ev)
     if (!e) TSQ_TRY(cudaEventCreate(&e));
 
@@ -195,6 +203,16 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   }
   b->cells = cells;
 
+  // The residues go up first, so the copy overlaps the planning below.  Any
+  // return from here on waits for it: the caller's buffer must outlive it.
+  TSQ_TRY(b->seqs.ensure(size_t(seqs_len) + 128));
+  TSQ_TRY(b->codes.ensure(size_t(seqs_len) + 128));
+  struct SyncOnExit {
+    cudaStream_t st;
+    ~SyncOnExit() { cudaStreamSynchronize(st); }
+  } sync_on_exit{b->stream};
+  if (seqs_len > 0) TSQ_TRY(cudaMemcpyAsync(b->seqs.p, seqs, size_t(seqs_len), cudaMemcpyHostToDevice, b->stream));
+
   // ---- lane types ------------------------------------------------------
   // Score fills run in int16x2 when the pair's values provably fit: the
   // upper bound max_score * min(m, n) (unchecked kernel) and the lower
@@ -220,6 +238,20 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
     lsel[size_t(k)] = lt;
     n_checked += lt == 2;
   }
+  // Long int32 pairs go to the CTA fill (their bands striped over 8 warps):
+  // those whose sweep on one 32-lane group -- ceil(m/256) bands of n+31
+  // steps -- would outlast the batch's balanced per-lane work (or, alone,
+  // 20,000 steps).
+  {
+    const double lanes = double(sms) * 24.0 * 32.0;
+    const double budget = std::max(20000.0, plain ? 0.0 : double(cells) / (lanes * kR));
+    for (int64_t k = 0; k < n; ++k) {
+      if (lsel[size_t(k)] != 0) continue;
+      const PairDev &pd = b->pairs_h[size_t(k)];
+      const double steps32 = double((pd.a_len + 255) / 256) * double(pd.b_len + 31);
+      if (pd.a_len > 0 && pd.b_len > 0 && steps32 > budget) lsel[size_t(k)] = 3;
+    }
+  }
 
   // ---- shapes and buckets ----------------------------------------------
   ShapeChooser ch;
@@ -236,8 +268,9 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   std::vector<int32_t> rsel(static_cast<size_t>(n));
   std::vector<int32_t> order(static_cast<size_t>(n));
   for (int64_t k = 0; k < n; ++k) {
-    const int rows_per_lane = lsel[size_t(k)] ? 2 * kR : kR;
+    const int rows_per_lane = (lsel[size_t(k)] == 1 || lsel[size_t(k)] == 2) ? 2 * kR : kR;
     Shape s = ch.pick(b->pairs_h[size_t(k)].a_len, b->pairs_h[size_t(k)].b_len, rows_per_lane);
+    if (lsel[size_t(k)] == 3) s = Shape{32, kR, 0};  // one 32-lane group per warp of the CTA
     s.i16 = 0;
     if (!shape_supported(s, b->out_mode, b->local)) return TSQ_E_INVALID_ARG;
     gsel[size_t(k)] = s.G;
@@ -245,22 +278,46 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
     order[size_t(k)] = int32_t(k);
   }
   // Bands and steps of a pair's sweep under its lane type and shape.
+  auto two_bands = [&](int32_t k) { return lsel[size_t(k)] == 1 || lsel[size_t(k)] == 2; };
   auto bands = [&](int32_t k) {
-    const int P = gsel[size_t(k)] * rsel[size_t(k)] * (lsel[size_t(k)] ? 2 : 1);
+    const int P = gsel[size_t(k)] * rsel[size_t(k)] * (two_bands(k) ? 2 : 1);
     return (b->pairs_h[size_t(k)].a_len + P - 1) / P;
   };
   auto steps = [&](int32_t k) {
-    return b->pairs_h[size_t(k)].b_len + gsel[size_t(k)] * (lsel[size_t(k)] ? 2 : 1) - 1;
+    return b->pairs_h[size_t(k)].b_len + gsel[size_t(k)] * (two_bands(k) ? 2 : 1) - 1;
   };
-  std::sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
-    if (lsel[size_t(x)] != lsel[size_t(y)]) return lsel[size_t(x)] > lsel[size_t(y)];
-    if (gsel[size_t(x)] != gsel[size_t(y)]) return gsel[size_t(x)] < gsel[size_t(y)];
-    const int bx = bands(x), by = bands(y);
-    if (bx != by) return bx > by;
-    const int nx = b->pairs_h[size_t(x)].b_len, ny = b->pairs_h[size_t(y)].b_len;
-    if (nx != ny) return nx > ny;
-    return x < y;
-  });
+  // Order: lane type (checked int16x2, int16x2, int32), then lane width,
+  // then bands and columns descending, then input order -- as one 44-bit
+  // key sorted by a stable LSD radix sort (O(n), the plan of an 8M-pair
+  // batch must not cost seconds).
+  {
+    std::vector<uint64_t> key(static_cast<size_t>(n));
+    for (int64_t k = 0; k < n; ++k) {
+      const int gi = gsel[size_t(k)] == 4 ? 0 : gsel[size_t(k)] == 8 ? 1 : gsel[size_t(k)] == 16 ? 2 : 3;
+      const uint64_t bandk = uint64_t(std::min(bands(int32_t(k)), (1 << 19) - 1));
+      const uint64_t colk = uint64_t(std::min(b->pairs_h[size_t(k)].b_len, (1 << 20) - 1));
+      static const uint64_t kLaneRank[4] = {3, 2, 1, 0};  // CTA, checked int16x2, int16x2, int32
+      key[size_t(k)] = (kLaneRank[lsel[size_t(k)]] << 42) | (uint64_t(gi) << 40) |
+                       (((1ull << 19) - 1 - bandk) << 20) | ((1ull << 20) - 1 - colk);
+    }
+    std::vector<int32_t> tmp(static_cast<size_t>(n));
+    std::vector<uint32_t> cnt(1u << 11);
+    for (int shift = 0; shift < 44; shift += 11) {  // 2 bits of lane rank above the 42 key bits
+      std::fill(cnt.begin(), cnt.end(), 0u);
+      for (int64_t q = 0; q < n; ++q) ++cnt[(key[size_t(order[size_t(q)])] >> shift) & 2047u];
+      uint32_t sum = 0;
+      for (uint32_t &c : cnt) {
+        const uint32_t v = c;
+        c = sum;
+        sum += v;
+      }
+      for (int64_t q = 0; q < n; ++q) {
+        const int32_t k = order[size_t(q)];
+        tmp[cnt[(key[size_t(k)] >> shift) & 2047u]++] = k;
+      }
+      order.swap(tmp);
+    }
+  }
 
   // One launch per lane type (int16x2 checked, int16x2, int32), each a list
   // of warp tasks -- consecutive pairs of one lane width, 32/G per warp --
@@ -278,6 +335,25 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
       ++e;
     }
     if (lt == 2) checked_begin = int32_t(s);
+    if (lt == 3) {
+      // One long pair per CTA; the CTAs pull pairs longest first.
+      Launch L;
+      L.R = kR;
+      L.i16 = 0;
+      L.cta = true;
+      L.task_begin = int32_t(s);
+      L.n_wtasks = int32_t(e - s);
+      const int max_blocks = cta_blocks(b->out_mode, b->local);
+      if (max_blocks <= 0) return TSQ_E_CUDA;
+      L.blocks = int32_t(std::max<int64_t>(1, std::min<int64_t>(max_blocks, e - s)));
+      L.bnd_cols = ((cols + 31) / 32 + 1) * 32;
+      L.bnd_offset = bnd_total;
+      bnd_total += int64_t(L.blocks) * L.bnd_cols * int64_t(cta_bnd_entry_bytes(b->out_mode));
+      bnd_total = (bnd_total + 255) & ~int64_t(255);
+      b->launches.push_back(L);
+      s = e;
+      continue;
+    }
     std::vector<int2> wt;
     std::vector<int64_t> wcost;
     for (int64_t q = s; q < e;) {
@@ -371,9 +447,8 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   // ---- device buffers and uploads -------------------------------------------
   uint8_t lut[256];
   build_lut(sc, lut);
-  // Staged code chunks read up to 64 bytes past a sequence.
-  TSQ_TRY(b->seqs.ensure(size_t(seqs_len) + 128));
-  TSQ_TRY(b->codes.ensure(size_t(seqs_len) + 128));
+  // (seqs and codes were sized above: staged code chunks read up to 64
+  // bytes past a sequence, hence the padding.)
   TSQ_TRY(b->pairs.ensure(sizeof(PairDev) * size_t(n)));
   TSQ_TRY(b->tasks.ensure(sizeof(int32_t) * size_t(n)));
   TSQ_TRY(b->res.ensure(sizeof(ResultDev) * size_t(n)));
@@ -399,7 +474,6 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
     TSQ_TRY(b->aln_h.ensure(size_t(b->aln_bytes)));
   }
   cudaStream_t st = b->stream;
-  if (seqs_len > 0) TSQ_TRY(cudaMemcpyAsync(b->seqs.p, seqs, size_t(seqs_len), cudaMemcpyHostToDevice, st));
   if (n > 0) {
     TSQ_TRY(cudaMemcpyAsync(b->pairs.p, b->pairs_h.data(), sizeof(PairDev) * size_t(n), cudaMemcpyHostToDevice, st));
     TSQ_TRY(cudaMemcpyAsync(b->tasks.p, order.data(), sizeof(int32_t) * size_t(n), cudaMemcpyHostToDevice, st));
@@ -439,8 +513,34 @@ int enqueue_run(tsq_batch *b) {
   TSQ_TRY(launch_encode(b->seqs.as<uint8_t>(), b->seqs_len, b->lut.as<uint8_t>(), b->codes.as<uint8_t>(), st));
   TSQ_TRY(record(b, 1));
   int32_t *rerun_count = b->counters.as<int32_t>() + nl + 1;
+  // The CTA launch (long pairs) runs on a side stream next to the others.
+  bool forked = false;
+  for (const Launch &L : b->launches) forked |= L.cta;
+  if (forked) {
+    TSQ_TRY(cudaEventRecord(b->ev_fork, st));
+    TSQ_TRY(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
+  }
   for (int l = 0; l < nl; ++l) {
     const Launch &L = b->launches[size_t(l)];
+    if (L.cta) {
+      FillArgs a{};
+      a.codes = b->codes.as<uint8_t>();
+      a.pairs = b->pairs.as<PairDev>();
+      a.tasks = b->tasks.as<int32_t>() + L.task_begin;
+      a.n_wtasks = L.n_wtasks;
+      a.counter = b->counters.as<int32_t>() + l;
+      a.matrix = b->matrix.as<int8_t>();
+      a.gap_open = b->params.gap_open;
+      a.gap_extend = b->params.gap_extend;
+      a.res = b->res.as<ResultDev>();
+      a.bnd = reinterpret_cast<int32_t *>(b->bnd.as<uint8_t>() + L.bnd_offset);
+      a.bnd_cols = L.bnd_cols;
+      a.planes = b->planes.as<uint8_t>();
+      a.plane_off = b->plane_off.as<int64_t>();
+      a.max_score = b->scheme.max_score;
+      TSQ_TRY(launch_cta(b->out_mode, b->local, a, L.blocks, b->side));
+      continue;
+    }
     if (L.rerun) {
       // Pairs the checked int16x2 launch flagged, compacted on the device.
       TSQ_TRY(launch_collect_overflow(b->tasks.as<int32_t>() + b->checked_begin, int32_t(b->n_checked),
@@ -466,6 +566,10 @@ int enqueue_run(tsq_batch *b) {
     a.overflow = b->overflow.as<int32_t>();
     a.max_score = b->scheme.max_score;
     TSQ_TRY(launch_fill(L.R, L.i16, b->out_mode, b->local, a, L.blocks, st));
+  }
+  if (forked) {
+    TSQ_TRY(cudaEventRecord(b->ev_join, b->side));
+    TSQ_TRY(cudaStreamWaitEvent(st, b->ev_join, 0));
   }
   if (b->n_checked > 0)
     TSQ_TRY(cudaMemcpyAsync(b->rerun_h.p, rerun_count, sizeof(int32_t), cudaMemcpyDeviceToHost, st));

@@ -46,6 +46,8 @@ struct PinBuf {
 struct Launch {
   int R = 8, i16 = 0;  // i16: 0 int32, 1 int16x2, 2 int16x2 with overflow check
   bool rerun = false;  // int32 re-run of flagged pairs (warp tasks built on the device)
+  bool cta = false;    // one long pair per CTA (fill_cta.cuh); pairs tasks[task_begin, +n_wtasks)
+  int32_t task_begin = 0;
   int32_t wt_begin = 0, n_wtasks = 0;  // slice of the warp-task list
   int32_t blocks = 0;
   int32_t bnd_cols = 0;
@@ -80,6 +82,8 @@ struct tsq_batch {
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   bool capturing = false;
   cudaEvent_t ev_fetch = nullptr;  // results copied to the pinned host buffers
+  cudaStream_t side = nullptr;     // the CTA launch runs here, forked from and joined to `stream`
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   tsq::Scheme scheme{};
   tsq_params params{};
   int out_mode = tsq::kOutScore;

@@ -111,6 +111,17 @@ __device__ __forceinline__ void stage_chunk(int k, int t, int nact, const Top *t
   }
 }
 
+// Only the code bytes of chunk k (for groups whose top row comes from
+// elsewhere): three 16-byte copies by lanes 0..2.
+template <int CODE_RING = kCodeRing>
+__device__ __forceinline__ void stage_codes(int k, int t, int nact, const uint8_t *codes, int64_t boff,
+                                            uint8_t *code_ring) {
+  const int c0 = kChunk * k;
+  if (c0 >= nact || t >= 3) return;
+  const int64_t a = ((boff + c0) & ~int64_t(15)) + 16 * t;
+  cp_async16(code_ring + (a & (CODE_RING - 1)), codes + a);
+}
+
 // ---- runtime lane width ----------------------------------------------------
 __device__ __forceinline__ unsigned group_mask_rt(int lane, int G) {
   return G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));

@@ -1,0 +1,55 @@
+// fill_cta.cu -- instantiations of the CTA-per-pair int32 fill.
+#include "fill_cta.cuh"
+
+namespace tsq {
+namespace fill {
+
+namespace {
+template <int OUT>
+cudaError_t go(bool local, const FillArgs &a, int blocks, cudaStream_t st) {
+  const size_t smem = cta_smem_bytes(OUT);
+  if (local)
+    fill_cta_kernel<true, OUT><<<blocks, kCtaThreads, smem, st>>>(a);
+  else
+    fill_cta_kernel<false, OUT><<<blocks, kCtaThreads, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int OUT>
+int occ(bool local) {
+  const size_t smem = cta_smem_bytes(OUT);
+  auto k = local ? fill_cta_kernel<true, OUT> : fill_cta_kernel<false, OUT>;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kCtaThreads, smem) != cudaSuccess) return 0;
+  return nb;
+}
+}  // namespace
+
+}  // namespace fill
+
+int cta_blocks(int out_mode, bool local) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int per_sm = 0;
+  switch (out_mode) {
+    case kOutScore: per_sm = fill::occ<kOutScore>(local); break;
+    case kOutIdent: per_sm = fill::occ<kOutIdent>(local); break;
+    case kOutTrace: per_sm = fill::occ<kOutTrace>(local); break;
+  }
+  return per_sm * sms;
+}
+
+size_t cta_bnd_entry_bytes(int out_mode) { return out_mode == kOutIdent ? 16 : 8; }
+
+cudaError_t launch_cta(int out_mode, bool local, const FillArgs &a, int blocks, cudaStream_t st) {
+  switch (out_mode) {
+    case kOutScore: return fill::go<kOutScore>(local, a, blocks, st);
+    case kOutIdent: return fill::go<kOutIdent>(local, a, blocks, st);
+    case kOutTrace: return fill::go<kOutTrace>(local, a, blocks, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace tsq

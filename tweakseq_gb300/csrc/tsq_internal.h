@@ -117,6 +117,11 @@ size_t fill_bnd_entry_bytes(int i16, int out_mode);
 cudaError_t launch_fill(int R, int i16, int out_mode, bool local, const FillArgs &a, int blocks,
                         cudaStream_t st);
 bool shape_supported(const Shape &sh, int out_mode, bool local);
+// One long pair per CTA (fill_cta.cu): FillArgs.tasks / n_wtasks hold the
+// pair list, bnd one wrap-around row of bnd_cols entries per block.
+int cta_blocks(int out_mode, bool local);
+size_t cta_bnd_entry_bytes(int out_mode);
+cudaError_t launch_cta(int out_mode, bool local, const FillArgs &a, int blocks, cudaStream_t st);
 cudaError_t launch_walk(const WalkArgs &a, cudaStream_t st);
 cudaError_t launch_encode(const uint8_t *seqs, int64_t len, const uint8_t *lut_dev, uint8_t *codes,
                           cudaStream_t st);
