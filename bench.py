@@ -58,6 +58,8 @@ def parse_args():
                     help="profiling case: only the batched leg over the first PAIRS pairs, no graph")
     ap.add_argument("--serve-requests", type=int, default=120, help="requests in the serving leg (0 = skip)")
     ap.add_argument("--serve-only", action="store_true", help="run only the serving leg and print it")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other configurations")
+    ap.add_argument("--configs-only", action="store_true", help="run only the other configurations")
     return ap.parse_args()
 
 
@@ -295,6 +297,7 @@ def run_ours(args):
         cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
     serving = serve_leg(args.serve_requests) if args.serve_requests > 0 else None
+    configs = configs_leg() if not args.no_configs else None
 
     clocks = clk.summary()
     line = {
@@ -316,6 +319,7 @@ def run_ours(args):
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
         "serving": serving,
+        "configs": configs,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -396,6 +400,75 @@ def serve_leg(n_requests=120, loads=(0.25, 0.5, 0.9), seed=5, plain_pairs=600):
     return out
 
 
+def configs_leg(c3_pairs=16):
+    """The other configurations, measured on the device (not the headline):
+    C1 all-vs-all 64 proteins with traceback (batched vs plain), a seeded
+    sample of C3 long DNA pairs with traceback, and C4 in full (7,998,000
+    pairs, score + identity).  Each is checked against the oracle."""
+    from oracle import oracle as O
+    from tweakseq_gb300 import aligner as A
+    from tweakseq_gb300 import workloads as W
+
+    out = {}
+    cores = O.num_cores()
+    # C1
+    ps = W.all_vs_all_proteins()
+    with A.Batch(ps, output="alignment", use_graph=True) as b:
+        for _ in range(3):
+            b.run()
+        ms = []
+        for _ in range(5):
+            b.run()
+            ms.append(b.stats()["device_ms"])
+        res = b.results()
+    t0 = time.perf_counter()
+    A.align_batch(ps, output="alignment")
+    e2e_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for k in range(len(ps)):
+        a, bb = ps.pair(k)
+        A.align_pair(a, bb, output="alignment")
+    plain_s = time.perf_counter() - t0
+    want, sa, sb = O.batch(ps.seqs, ps.a_off, ps.a_len, ps.b_off, ps.b_len, mode=O.MODE_ALIGN, strings=True,
+                           nthreads=cores)
+    mism = int(sum((res.table[f] != want[f]).sum() for f in ("score", "n_ident", "n_cols")))
+    mism += sum(x != y for x, y in zip(res.aln_a, sa)) + sum(x != y for x, y in zip(res.aln_b, sb))
+    out["all_vs_all_64_proteins"] = {
+        "pairs": len(ps), "cells": ps.cells, "output": "alignment (global, BLOSUM62 11/1)",
+        "batched_gcups": ps.cells / (float(np.median(ms)) * 1e-3) / 1e9, "e2e_gcups": ps.cells / e2e_s / 1e9,
+        "plain_gcups": ps.cells / plain_s / 1e9, "mismatches_vs_oracle": mism}
+    # C3 sample
+    ps = W.long_dna_pairs(c3_pairs)
+    with A.Batch(ps, matrix="dna", gap_open=5, gap_extend=2, output="alignment", use_graph=True) as b:
+        b.run()
+        b.run()
+        st = b.stats()
+        res = b.results()
+    want = O.batch(ps.seqs, ps.a_off, ps.a_len, ps.b_off, ps.b_len, O.DNA, 5, 2, False, O.MODE_IDENT, cores)
+    mism = int(sum((res.table[f] != want[f]).sum() for f in ("score", "n_ident", "n_cols")))
+    out["long_dna_pairs_sample"] = {
+        "pairs": len(ps), "cells": ps.cells, "output": "alignment (global, +2/-3, gap 5/2)",
+        "sample": f"{c3_pairs} of the 1,000 pairs (seed 3); the full set needs ~500 GB of traceback planes",
+        "batched_gcups": ps.cells / (st["device_ms"] * 1e-3) / 1e9, "fill_gcups": ps.cells / (st["fill_ms"] * 1e-3) / 1e9,
+        "mismatches_vs_oracle": mism, "checked": "score, n_ident, n_cols"}
+    # C4 full
+    ps = W.guide_tree_families()
+    with A.Batch(ps, output="identity", use_graph=True) as b:
+        b.run()
+        b.run()
+        st = b.stats()
+        res = b.results()
+    idx = np.random.default_rng(4).choice(len(ps), 4000, replace=False)
+    sub = ps.subset(idx)
+    want = O.batch(sub.seqs, sub.a_off, sub.a_len, sub.b_off, sub.b_len, mode=O.MODE_IDENT, nthreads=cores)
+    mism = int(sum((res.table[f][idx] != want[f]).sum() for f in ("score", "n_ident", "n_cols")))
+    out["guide_tree_all_vs_all"] = {
+        "pairs": len(ps), "cells": ps.cells, "output": "score + identity (global, BLOSUM62 11/1)",
+        "batched_gcups": ps.cells / (st["device_ms"] * 1e-3) / 1e9, "fill_gcups": ps.cells / (st["fill_ms"] * 1e-3) / 1e9,
+        "mismatches_vs_oracle": mism, "checked": "4,000 seeded pairs"}
+    return out
+
+
 def run_profile(args):
     """Small case for ncu: the device-resident batch over a prefix of the
     workload, launched without a graph so each kernel is a separate launch."""
@@ -421,6 +494,11 @@ def main():
     args = parse_args()
     if args.profile:
         run_profile(args)
+        return
+    if args.configs_only:
+        from tweakseq_gb300 import build as B
+        B.build()
+        print(json.dumps({"configs": configs_leg()}), flush=True)
         return
     if args.serve_only:
         from tweakseq_gb300 import build as B

@@ -208,37 +208,45 @@ def guide_tree_families(n_families: int = 20, per_family: int = 200, lo: int = 2
                         indel: float = 0.03, seed: int = 4, all_pairs: bool = True) -> PairSet:
     """Protein families evolved down random binary trees; all-vs-all.
 
-    Each family gets a per-branch substitution rate drawn so that leaf pairs
-    land at roughly 20-60 % identity; 3 % of leaf residues carry indels
-    (spread over the branches)."""
+    Each family is an ultrametric random binary tree: the root sits at
+    divergence 0.8 (expected substitutions per site from any leaf), every
+    internal node somewhere between its parent and 0.26, leaves at 0.  A
+    branch of length L replaces each residue with probability 1 - exp(-L)
+    and carries indels in proportion to L (3 % over a root-to-leaf path).
+    Two leaves differ by twice the height of their last common ancestor, so
+    leaf pairs of a family fall between about 20 % identity (ancestor at the
+    root) and 60 % (ancestor at 0.26); pairs from different families are
+    unrelated."""
     rng = np.random.default_rng(seed)
     leaves = []
     same = float(np.sum(AA_FREQ ** 2))
+    h_root, h_floor = 0.8, 0.26
+
+    def branch(seq, length):
+        p_sub = (1.0 - np.exp(-length)) / (1.0 - same)
+        child, _ = _mutate_proteins(rng, seq, np.array([len(seq)]), np.array([min(1.0, p_sub)]),
+                                    indel * length / h_root)
+        return child if len(child) else random_protein(rng, 1)
+
+    def grow(seq, k, h):
+        if k == 1:
+            leaves.append(seq.tobytes())
+            return
+        k1 = int(rng.integers(1, k))
+        for kk in (k1, k - k1):
+            h_child = 0.0 if kk == 1 else h - rng.uniform(0.0, 0.5) * (h - h_floor)
+            grow(branch(seq, h - h_child), kk, h_child)
+
     for _ in range(n_families):
-        root = random_protein(rng, int(rng.integers(lo, hi + 1)))
-        rate = rng.uniform(0.035, 0.075)
-        depth_guess = 2.0 * np.log(per_family)
-        br_indel = indel / depth_guess
-
-        def grow(seq, k):
-            if k == 1:
-                leaves.append(seq.tobytes())
-                return
-            k1 = int(rng.integers(1, k))
-            for kk in (k1, k - k1):
-                child, _ = _mutate_proteins(rng, seq, np.array([len(seq)]), np.array([rate / (1 - same)]), br_indel)
-                if len(child) == 0:
-                    child = random_protein(rng, 1)
-                grow(child, kk)
-
-        grow(root, per_family)
+        grow(random_protein(rng, int(rng.integers(lo, hi + 1))), per_family, h_root)
     n = len(leaves)
     if all_pairs:
         iu, ju = np.triu_indices(n, k=1)
         pairs = np.stack([iu, ju], 1)
     else:
         pairs = np.zeros((0, 2), dtype=np.int64)
-    ps = _pairset_from_lists(leaves, pairs, name=f"guide_tree_{n}", meta={"seed": seed, "families": n_families})
+    ps = _pairset_from_lists(leaves, pairs, name=f"guide_tree_{n}",
+                             meta={"seed": seed, "families": n_families, "per_family": per_family})
     ps.meta["n_seqs"] = n
     return ps
 
