@@ -60,6 +60,7 @@ def parse_args():
     ap.add_argument("--serve-only", action="store_true", help="run only the serving leg and print it")
     ap.add_argument("--no-configs", action="store_true", help="skip the other configurations")
     ap.add_argument("--configs-only", action="store_true", help="run only the other configurations")
+    ap.add_argument("--msa-only", action="store_true", help="run only the consensus and guide-tree legs")
     return ap.parse_args()
 
 
@@ -298,6 +299,7 @@ def run_ours(args):
 
     serving = serve_leg(args.serve_requests) if args.serve_requests > 0 else None
     configs = configs_leg() if not args.no_configs else None
+    msa_steps = msa_leg() if not args.no_configs else None
 
     clocks = clk.summary()
     line = {
@@ -320,6 +322,7 @@ def run_ours(args):
         "clocks": clocks,
         "serving": serving,
         "configs": configs,
+        "msa": msa_steps,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -469,6 +472,100 @@ def configs_leg(c3_pairs=16):
     return out
 
 
+def msa_leg(cpu_cols=40, cpu_tree_leaves=1000):
+    """The steps either side of the pairwise path: the consensus line of a
+    4,000 x 1,000 and a 100,000 x 2,000 alignment (HBM-bound count pass),
+    and UPGMA / NJ guide trees of the 4,000-sequence guide-tree workload
+    built from its device-resident all-vs-all identities."""
+    import torch
+
+    from oracle import oracle as O
+    from tweakseq_gb300 import _native as N
+    from tweakseq_gb300 import aligner as A
+    from tweakseq_gb300 import msa
+    from tweakseq_gb300 import workloads as W
+
+    out = {}
+    L = N.lib()
+    peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"] if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else 6800.0
+    for nseq, ncols in ((4000, 1000), (100_000, 2000)):
+        rng = np.random.default_rng(nseq)
+        # Columns with a favourite residue (kept in 60 % of rows), 15 % gaps.
+        fav = W.random_protein(rng, ncols)
+        rows = W.AA_LETTERS[rng.integers(0, 20, size=(nseq, ncols), dtype=np.uint8)]
+        u = rng.integers(0, 100, size=(nseq, ncols), dtype=np.uint8)
+        rows = np.where(u < 60, fav[None, :], rows)
+        rows[u >= 85] = ord("-")
+        rows = np.ascontiguousarray(rows, dtype=np.uint8)
+        d_rows = torch.from_numpy(rows).cuda()
+        d_out = torch.zeros(ncols, dtype=torch.uint8, device="cuda")
+        nb = L.tsq_consensus_scratch_bytes(ncols)
+        scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        st = torch.cuda.current_stream()
+        ms = []
+        for it in range(13):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            rc = L.tsq_consensus_device(d_rows.data_ptr(), nseq, ncols, ncols, -1.0, d_out.data_ptr(), None, None,
+                                        scratch.data_ptr(), nb, st.cuda_stream)
+            e1.record(st)
+            assert rc == 0
+            st.synchronize()
+            if it >= 3:
+                ms.append(e0.elapsed_time(e1))
+        dev_ms = float(np.median(ms))
+        t0 = time.perf_counter()
+        got = msa.consensus(rows)
+        host_ms = (time.perf_counter() - t0) * 1e3
+        # The reference's algorithm (O(nseq^2) per column) on a column sample.
+        cols = np.random.default_rng(1).choice(ncols, min(cpu_cols, ncols), replace=False)
+        sub = np.ascontiguousarray(rows[:, cols]) if nseq <= 4000 else np.ascontiguousarray(rows[:4000, cols])
+        t0 = time.perf_counter()
+        want = O.consensus(sub)
+        cpu_s = time.perf_counter() - t0
+        ok = bytes(got.sequence[c] for c in cols) == want[0] if nseq <= 4000 else None
+        pair_ops = float(sub.shape[0]) ** 2 * sub.shape[1]
+        bytes_ = nseq * ncols
+        out[f"consensus_{nseq}x{ncols}"] = {
+            "device_ms": dev_ms, "host_api_ms": host_ms, "gbs": bytes_ / (dev_ms * 1e-3) / 1e9,
+            "roofline": {"bound": "hbm", "achieved": bytes_ / (dev_ms * 1e-3) / 1e9, "peak": peak,
+                         "frac": bytes_ / (dev_ms * 1e-3) / 1e9 / peak, "unit": "GB/s",
+                         "bytes_per_launch": bytes_},
+            "cpu_reference_algorithm": {"columns_per_s": sub.shape[1] / cpu_s,
+                                        "row_pairs_per_s": pair_ops / cpu_s, "cores": O.num_cores(),
+                                        "sample": f"{sub.shape[1]} columns x {sub.shape[0]} rows"},
+            "cpu_extrapolated_s": cpu_s * (float(nseq) ** 2 * ncols) / pair_ops,
+            "bitexact_sample": ok}
+        del d_rows, scratch, flush
+    # Guide trees of the 4,000-sequence all-vs-all.
+    ps = W.guide_tree_families()
+    n = int(ps.meta["n_seqs"])
+    with A.Batch(ps, output="identity") as b:
+        b.run()
+        res = b.results()
+        for method in ("upgma", "nj"):
+            msa.guide_tree_from_batch(b, n, method)  # warm
+            t0 = time.perf_counter()
+            tree = msa.guide_tree_from_batch(b, n, method)
+            tree_ms = (time.perf_counter() - t0) * 1e3
+            D = O.identity_distances(n, res.table["n_ident"], res.table["n_cols"])
+            want = O.guide_tree(D, N.TREE[method])
+            same = all(np.array_equal(tree.nodes[f], want[f]) for f in N.TREE_NODE_DTYPE.names)
+            k = cpu_tree_leaves
+            t0 = time.perf_counter()
+            O.guide_tree(np.ascontiguousarray(D[:k, :k]), N.TREE[method])
+            cpu_s = time.perf_counter() - t0
+            out[f"guide_tree_{method}_{n}"] = {
+                "ms": tree_ms, "joins": n - 1, "bitexact_vs_oracle": bool(same),
+                "what": "from the batch's device-resident identities: distances, n-1 join launches, joins to host",
+                "cpu_oracle_s_at_1000_leaves": cpu_s,
+                "cpu_oracle_s_extrapolated": cpu_s * (n / k) ** 3}
+    return out
+
+
 def run_profile(args):
     """Small case for ncu: the device-resident batch over a prefix of the
     workload, launched without a graph so each kernel is a separate launch."""
@@ -499,6 +596,11 @@ def main():
         from tweakseq_gb300 import build as B
         B.build()
         print(json.dumps({"configs": configs_leg()}), flush=True)
+        return
+    if args.msa_only:
+        from tweakseq_gb300 import build as B
+        B.build()
+        print(json.dumps({"msa": msa_leg()}), flush=True)
         return
     if args.serve_only:
         from tweakseq_gb300 import build as B

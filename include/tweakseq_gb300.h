@@ -252,6 +252,81 @@ int tsq_align_score_noalloc(const uint8_t *d_seqs, int64_t seqs_len,
                             int32_t max_len, const tsq_params *p,
                             tsq_device_result *d_out, void *stream);
 
+/* ---- Consensus line -------------------------------------------------------- */
+
+/* Consensus of a gapped alignment; replaces Consensus::calculate
+ * (tweakseq/Core/Annotations/Consensus.cpp:80-161, called from
+ * Project::setAligned, tweakseq/Core/Project.cpp:112-121).  rows: nseq rows
+ * of ncols bytes, row k at rows + k*stride (the low byte of each residue, as
+ * the reference reads it).  For each column every row is scored against
+ * every other row -- +1 when both bytes are outside 'A'..'Z' (a gap pair,
+ * counted as a match), -4 when one is, else BLOSUM62 (a match when
+ * positive; J, O, U share the X row) -- and the first row with the highest
+ * sum wins.  consensus[c] is that row's byte when its match count is >=
+ * plurality, else '?'.  plurality < 0 selects the reference's default,
+ * nseq / 2 (Consensus::setSequences, Consensus.cpp:163-172).  best_score and
+ * best_matches (either may be NULL) receive the winning row's figures.
+ * Host buffers; the call copies in, computes and copies out. */
+int tsq_consensus(const uint8_t *rows, int32_t nseq, int32_t ncols,
+                  int64_t stride, double plurality, uint8_t *consensus,
+                  int32_t *best_score, int32_t *best_matches);
+
+/* Device-buffer form of tsq_consensus: everything already in device memory,
+ * scratch of tsq_consensus_scratch_bytes(ncols) bytes supplied by the
+ * caller, kernels enqueued on `stream` (cudaStream_t) without waiting.
+ * Allocates nothing. */
+size_t tsq_consensus_scratch_bytes(int32_t ncols);
+int tsq_consensus_device(const uint8_t *d_rows, int32_t nseq, int32_t ncols,
+                         int64_t stride, double plurality,
+                         uint8_t *d_consensus, int32_t *d_best_score,
+                         int32_t *d_best_matches, void *d_scratch,
+                         size_t scratch_bytes, void *stream);
+
+/* ---- Guide trees ------------------------------------------------------------- */
+
+/* The tree step the external multiple aligners run after all-vs-all
+ * (ClustalO is asked for tree order, tweakseq/Core/ClustalO.cpp:51); the
+ * reference has no tree code of its own.  UPGMA or neighbour joining over
+ * integer distances in units of 2^-32: d = floor((n_cols - n_ident) * 2^32
+ * / n_cols), 2^32 when n_cols is 0.  Clusters hold positions 0..n-1; each
+ * step joins the pair (i < j) with the smallest criterion (UPGMA: D(i,j);
+ * NJ: (m-2) D(i,j) - r_i - r_j with r the row sums over the m active
+ * clusters), ties to the smallest i then j; the join takes position i.
+ * UPGMA: D(u,k) = floor((s_i D(i,k) + s_j D(j,k)) / (s_i + s_j)),
+ * height floor(D(i,j)/2).  NJ: D(u,k) = floor((D(i,k) + D(j,k) - D(i,j))/2),
+ * branch of i floor(((m-2) D(i,j) + r_i - r_j) / (2(m-2))) (floor(D(i,j)/2)
+ * when m = 2), branch of j = D(i,j) minus that.  Join t is node n + t;
+ * leaves are nodes 0..n-1.  n <= 65,535. */
+#define TSQ_TREE_UPGMA 0
+#define TSQ_TREE_NJ 1
+
+typedef struct tsq_tree_node {
+  int32_t left, right;   /* child node ids */
+  int32_t size;          /* leaves under the join */
+  int32_t pos;           /* position the join takes */
+  int64_t dist;          /* D(left, right) when joined (2^-32 units) */
+  int64_t height;        /* UPGMA height (2^-32 units); 0 for NJ */
+  int64_t left_length;   /* branch lengths (2^-32 units) */
+  int64_t right_length;
+} tsq_tree_node;
+
+/* From a symmetric n x n distance matrix (row-major, 2^-32 units; the
+ * diagonal is ignored).  out: n - 1 joins. */
+int tsq_guide_tree_dist(int32_t n, const int64_t *dist, int32_t method,
+                        tsq_tree_node *out);
+
+/* From identities of the n(n-1)/2 unordered pairs (i < j) in row-major
+ * order: (0,1), (0,2), ..., (0,n-1), (1,2), ... */
+int tsq_guide_tree(int32_t n, const int32_t *n_ident, const int32_t *n_cols,
+                   int32_t method, tsq_tree_node *out);
+
+/* From a batch that has run: its pairs must be the all-vs-all of n
+ * sequences in the order above (pair (i,j) aligns sequence i as a against
+ * sequence j as b) with TSQ_OUT_IDENTITY or TSQ_OUT_ALIGNMENT.  The
+ * identities stay in device memory; only the joins come back. */
+int tsq_batch_guide_tree(tsq_batch *b, int32_t n, int32_t method,
+                         tsq_tree_node *out);
+
 /* ---- Device probe ---------------------------------------------------------- */
 
 /* Measured rate of the DP fill's DPX-class instructions (add-then-max and

@@ -75,6 +75,10 @@ def lib():
         L.tsqo_batch.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int64, ctypes.POINTER(Scheme), i32, i32, i32,
                                  i32, i32, vp, vp, vp, vp]
         L.tsqo_num_cores.restype = ctypes.c_int
+        L.tsqo_consensus.argtypes = [vp, i32, i32, ctypes.c_int64, ctypes.c_double, i32, vp, vp, vp]
+        L.tsqo_identity_distance.argtypes = [i32, i32]
+        L.tsqo_identity_distance.restype = ctypes.c_int64
+        L.tsqo_guide_tree.argtypes = [i32, vp, i32, vp]
         _lib = L
     return _lib
 
@@ -213,3 +217,51 @@ def batch(seqs: np.ndarray, a_off, a_len, b_off, b_len, which=BLOSUM62, gap_open
         sa.append(aln_a[o:o + L].tobytes().decode())
         sb.append(aln_b[o:o + L].tobytes().decode())
     return out, sa, sb
+
+
+def consensus(rows: np.ndarray, plurality: float = -1.0, nthreads: int = 0):
+    """Consensus::calculate restated (tsqo_consensus) over a 2-D uint8 array
+    (one row per sequence).  Returns (consensus bytes, best_score,
+    best_matches)."""
+    rows = np.ascontiguousarray(rows, dtype=np.uint8)
+    nseq, ncols = rows.shape
+    out = np.zeros(max(ncols, 1), dtype=np.uint8)
+    sc = np.zeros(max(ncols, 1), dtype=np.int32)
+    mt = np.zeros(max(ncols, 1), dtype=np.int32)
+    rc = lib().tsqo_consensus(rows.ctypes.data, nseq, ncols, ncols, plurality, nthreads, out.ctypes.data,
+                              sc.ctypes.data, mt.ctypes.data)
+    if rc:
+        raise OracleError(rc)
+    return out[:ncols].tobytes(), sc[:ncols], mt[:ncols]
+
+
+TREE_UPGMA, TREE_NJ = 0, 1
+DIST_ONE = 1 << 32
+TREE_NODE_DTYPE = np.dtype([("left", np.int32), ("right", np.int32), ("size", np.int32), ("pos", np.int32),
+                            ("dist", np.int64), ("height", np.int64), ("left_length", np.int64),
+                            ("right_length", np.int64)])
+
+
+def identity_distances(n: int, n_ident, n_cols) -> np.ndarray:
+    """Full n x n int64 distance matrix (2^-32 units) from the identities of
+    the unordered pairs (i < j) in row-major order."""
+    n_ident = np.asarray(n_ident, dtype=np.int64)
+    n_cols = np.asarray(n_cols, dtype=np.int64)
+    num = (n_cols - n_ident).astype(np.uint64) << np.uint64(32)
+    d = np.where(n_cols > 0, num // np.maximum(n_cols, 1).astype(np.uint64), np.uint64(DIST_ONE)).astype(np.int64)
+    D = np.zeros((n, n), dtype=np.int64)
+    iu = np.triu_indices(n, 1)
+    D[iu] = d
+    D.T[iu] = d
+    return D
+
+
+def guide_tree(dist: np.ndarray, method: int = TREE_UPGMA) -> np.ndarray:
+    """tsqo_guide_tree over a full symmetric int64 matrix; n-1 joins."""
+    dist = np.ascontiguousarray(dist, dtype=np.int64)
+    n = dist.shape[0]
+    out = np.zeros(max(n - 1, 1), dtype=TREE_NODE_DTYPE)
+    rc = lib().tsqo_guide_tree(n, dist.ctypes.data, method, out.ctypes.data)
+    if rc:
+        raise OracleError(rc)
+    return out[:max(n - 1, 0)]

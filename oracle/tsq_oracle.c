@@ -610,3 +610,200 @@ int tsqo_batch(const uint8_t *seqs, const int64_t *a_off, const int32_t *a_len,
   free(th);
   return atomic_load(&J.status);
 }
+
+/* ------------------------------------------------------------------------
+ * Consensus of a gapped alignment: Consensus::calculate restated loop for
+ * loop (tweakseq/Core/Annotations/Consensus.cpp:80-161), O(ncols * nseq^2),
+ * doubles as there, one column per task over POSIX threads.
+ * ---------------------------------------------------------------------- */
+
+/* Residue byte -> BLOSUM62 row, 99 for anything outside 'A'..'Z'
+ * (Consensus.cpp:96-106; the map of :61-69 sends J, O, U, X to 22). */
+static int consensus_class(uint8_t byte) {
+  const int idx = (int)byte - 65;
+  if (idx < 0 || idx > 25) return 99;
+  return b62_index((char)byte);
+}
+
+typedef struct {
+  const uint8_t *rows;
+  int32_t nseq, ncols;
+  int64_t stride;
+  double plurality;
+  uint8_t *out;
+  int32_t *best_score, *best_matches;
+  atomic_llong next;
+} consensus_job;
+
+static void consensus_column(const consensus_job *J, int32_t c) {
+  double hi_score = 0.0, ri_matches = 0.0;
+  int32_t ri_hi = 0;
+  for (int32_t ri = 0; ri < J->nseq; ++ri) {
+    double score = 0.0, matches = 0.0;
+    const int resi = consensus_class(J->rows[(int64_t)ri * J->stride + c]);
+    for (int32_t rj = 0; rj < J->nseq; ++rj) {
+      if (ri == rj) continue;
+      const double weight = 1.0;
+      const int resj = consensus_class(J->rows[(int64_t)rj * J->stride + c]);
+      if (resi == 99 && resj == 99) {
+        score += weight;
+        if (weight > 0) matches += weight;
+      } else if (resi == 99 || resj == 99) {
+        score += -4 * weight;
+      } else {
+        const double tmp = kB62[resi][resj] * weight;
+        score += tmp;
+        if (tmp > 0) matches += weight;
+      }
+    }
+    if (ri == 0 || score > hi_score) {
+      hi_score = score;
+      ri_hi = ri;
+      ri_matches = matches;
+    }
+  }
+  J->out[c] = ri_matches >= J->plurality ? J->rows[(int64_t)ri_hi * J->stride + c] : (uint8_t)'?';
+  if (J->best_score) J->best_score[c] = (int32_t)hi_score;
+  if (J->best_matches) J->best_matches[c] = (int32_t)ri_matches;
+}
+
+static void *consensus_worker(void *arg) {
+  consensus_job *J = (consensus_job *)arg;
+  for (;;) {
+    const int64_t c = atomic_fetch_add(&J->next, 1);
+    if (c >= J->ncols) break;
+    consensus_column(J, (int32_t)c);
+  }
+  return NULL;
+}
+
+int tsqo_consensus(const uint8_t *rows, int32_t nseq, int32_t ncols, int64_t stride, double plurality,
+                   int32_t nthreads, uint8_t *out, int32_t *best_score, int32_t *best_matches) {
+  if (nseq <= 0 || ncols < 0 || stride < ncols || !rows || (!out && ncols)) return TSQO_E_INVALID_ARG;
+  consensus_job J;
+  memset(&J, 0, sizeof(J));
+  J.rows = rows;
+  J.nseq = nseq;
+  J.ncols = ncols;
+  J.stride = stride;
+  /* Consensus::setSequences: plurality = (sum of unit weights) / 2. */
+  J.plurality = plurality < 0 ? nseq / 2.0 : plurality;
+  J.out = out;
+  J.best_score = best_score;
+  J.best_matches = best_matches;
+  atomic_init(&J.next, 0);
+  if (nthreads <= 0) nthreads = tsqo_num_cores();
+  if (nthreads > ncols) nthreads = ncols > 0 ? ncols : 1;
+  pthread_t *th = malloc(sizeof(pthread_t) * (size_t)nthreads);
+  if (!th) return TSQO_E_NOMEM;
+  int started = 0;
+  for (int t = 1; t < nthreads; ++t)
+    if (pthread_create(&th[started], NULL, consensus_worker, &J) == 0) ++started;
+  consensus_worker(&J);
+  for (int t = 0; t < started; ++t) pthread_join(th[t], NULL);
+  free(th);
+  return TSQO_OK;
+}
+
+/* ------------------------------------------------------------------------
+ * Guide tree from all-vs-all identities: UPGMA (Sokal & Michener 1958) or
+ * neighbour joining (Saitou & Nei 1987, in the Studier & Keppler 1988 form)
+ * over integer fixed-point distances, with the conventions of
+ * tsq_oracle.h.  Plain O(n^3): every step scans every active pair.
+ * ---------------------------------------------------------------------- */
+
+int64_t tsqo_identity_distance(int32_t n_ident, int32_t n_cols) {
+  if (n_cols <= 0) return TSQO_DIST_ONE;
+  return (int64_t)(((uint64_t)(uint32_t)(n_cols - n_ident) << 32) / (uint64_t)(uint32_t)n_cols);
+}
+
+static int64_t floor_div(int64_t a, int64_t b) {
+  int64_t q = a / b;
+  if ((a % b != 0) && ((a < 0) != (b < 0))) --q;
+  return q;
+}
+
+int tsqo_guide_tree(int32_t n, const int64_t *dist, int32_t method, tsqo_tree_node *out) {
+  if (n < 1 || !dist || (method != TSQO_TREE_UPGMA && method != TSQO_TREE_NJ) || (!out && n > 1))
+    return TSQO_E_INVALID_ARG;
+  int64_t *D = malloc(sizeof(int64_t) * (size_t)n * (size_t)n);
+  int64_t *r = malloc(sizeof(int64_t) * (size_t)n);
+  int64_t *height = malloc(sizeof(int64_t) * (size_t)n);
+  int32_t *node = malloc(sizeof(int32_t) * (size_t)n), *size = malloc(sizeof(int32_t) * (size_t)n);
+  uint8_t *active = malloc((size_t)n);
+  if (!D || !r || !height || !node || !size || !active) {
+    free(D), free(r), free(height), free(node), free(size), free(active);
+    return TSQO_E_NOMEM;
+  }
+  memcpy(D, dist, sizeof(int64_t) * (size_t)n * (size_t)n);
+  for (int32_t i = 0; i < n; ++i) {
+    node[i] = i;
+    size[i] = 1;
+    height[i] = 0;
+    active[i] = 1;
+    r[i] = 0;
+    for (int32_t k = 0; k < n; ++k)
+      if (k != i) r[i] += D[(int64_t)i * n + k];
+  }
+  int32_t m = n;
+  for (int32_t t = 0; t < n - 1; ++t, --m) {
+    int32_t bi = -1, bj = -1;
+    int64_t best = 0;
+    for (int32_t i = 0; i < n; ++i) {
+      if (!active[i]) continue;
+      for (int32_t j = i + 1; j < n; ++j) {
+        if (!active[j]) continue;
+        const int64_t dij = D[(int64_t)i * n + j];
+        const int64_t c = method == TSQO_TREE_UPGMA ? dij : (int64_t)(m - 2) * dij - r[i] - r[j];
+        if (bi < 0 || c < best) { /* strict: the first pair in (i, j) order wins ties */
+          best = c;
+          bi = i;
+          bj = j;
+        }
+      }
+    }
+    const int64_t dij = D[(int64_t)bi * n + bj];
+    tsqo_tree_node *o = &out[t];
+    o->left = node[bi];
+    o->right = node[bj];
+    o->size = size[bi] + size[bj];
+    o->pos = bi;
+    o->dist = dij;
+    if (method == TSQO_TREE_UPGMA) {
+      const int64_t h = dij >> 1;
+      o->height = h;
+      o->left_length = h - height[bi];
+      o->right_length = h - height[bj];
+      height[bi] = h;
+    } else {
+      o->height = 0;
+      if (m > 2) {
+        o->left_length = floor_div((int64_t)(m - 2) * dij + r[bi] - r[bj], 2 * (int64_t)(m - 2));
+      } else {
+        o->left_length = dij >> 1;
+      }
+      o->right_length = dij - o->left_length;
+    }
+    /* Join: the new cluster takes position bi, position bj leaves. */
+    int64_t r_new = 0;
+    for (int32_t k = 0; k < n; ++k) {
+      if (!active[k] || k == bi || k == bj) continue;
+      const int64_t dik = D[(int64_t)bi * n + k], djk = D[(int64_t)bj * n + k];
+      int64_t du;
+      if (method == TSQO_TREE_UPGMA)
+        du = floor_div((int64_t)size[bi] * dik + (int64_t)size[bj] * djk, (int64_t)(size[bi] + size[bj]));
+      else
+        du = (dik + djk - dij) >> 1;
+      r[k] += du - dik - djk;
+      r_new += du;
+      D[(int64_t)bi * n + k] = du;
+      D[(int64_t)k * n + bi] = du;
+    }
+    r[bi] = r_new;
+    node[bi] = n + t;
+    size[bi] += size[bj];
+    active[bj] = 0;
+  }
+  free(D), free(r), free(height), free(node), free(size), free(active);
+  return TSQO_OK;
+}

@@ -123,6 +123,57 @@ int tsqo_batch(const uint8_t *seqs, const int64_t *a_off, const int32_t *a_len,
 /* Number of online cores the batch driver uses by default. */
 int tsqo_num_cores(void);
 
+/* Consensus of a gapped alignment, restated loop for loop from
+ * Consensus::calculate (tweakseq/Core/Annotations/Consensus.cpp:80-161):
+ * rows holds nseq rows of ncols bytes (row k at rows + k*stride).  For each
+ * column, every row ri scores the sum over the other rows rj of: +1 when
+ * both bytes are outside 'A'..'Z' (a "gap" pair, counted as a match), -4
+ * when exactly one is, else BLOSUM62[ri][rj] (counted as a match when
+ * positive; J, O, U, X share the X row).  The first row with the highest
+ * score wins; the column's consensus is that row's byte when its match count
+ * is >= plurality, else '?'.  plurality < 0 means the reference's default,
+ * nseq / 2 (Consensus::setSequences, Consensus.cpp:163-172).  best_score and
+ * best_matches (either may be NULL) receive the winning row's figures. */
+int tsqo_consensus(const uint8_t *rows, int32_t nseq, int32_t ncols, int64_t stride, double plurality,
+                   int32_t nthreads, uint8_t *out, int32_t *best_score, int32_t *best_matches);
+
+/* Guide trees from all-vs-all identities.
+ *
+ * Conventions (the CUDA library reproduces every one bit for bit):
+ *   - Distances are integers in units of 2^-32: d = floor((n_cols - n_ident)
+ *     * 2^32 / n_cols), 2^32 when n_cols is 0 (tsqo_identity_distance).
+ *     Integer arithmetic makes every step exact and order-independent.
+ *   - Clusters sit at positions 0..n-1 (leaf k at position k).  Each step
+ *     joins the active pair (i < j) with the smallest criterion; ties go to
+ *     the smallest i, then the smallest j.  The join takes position i, j
+ *     leaves.  Join t (0-based) is node n + t; leaves are nodes 0..n-1.
+ *   - UPGMA: criterion D(i,j); D(u,k) = floor((s_i D(i,k) + s_j D(j,k)) /
+ *     (s_i + s_j)) with s the cluster sizes; height(u) = floor(D(i,j) / 2);
+ *     branch length = height(u) - height(child).
+ *   - NJ: with m active clusters and r_k = sum over active l != k of D(k,l),
+ *     criterion (m - 2) D(i,j) - r_i - r_j; D(u,k) = floor((D(i,k) + D(j,k)
+ *     - D(i,j)) / 2); branch length of i = floor(((m - 2) D(i,j) + r_i -
+ *     r_j) / (2 (m - 2))) (floor(D(i,j) / 2) when m = 2), of j = D(i,j) minus
+ *     that. */
+#define TSQO_DIST_ONE ((int64_t)1 << 32)
+#define TSQO_TREE_UPGMA 0
+#define TSQO_TREE_NJ 1
+
+typedef struct {
+  int32_t left, right; /* node ids */
+  int32_t size;        /* leaves under the join */
+  int32_t pos;         /* position the join takes */
+  int64_t dist;        /* D(left, right) when joined */
+  int64_t height;      /* UPGMA height, 0 for NJ */
+  int64_t left_length, right_length;
+} tsqo_tree_node;
+
+int64_t tsqo_identity_distance(int32_t n_ident, int32_t n_cols);
+
+/* dist: n*n row-major, symmetric (the diagonal is ignored).  out: n-1
+ * joins.  One leaf gives no joins. */
+int tsqo_guide_tree(int32_t n, const int64_t *dist, int32_t method, tsqo_tree_node *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,7 +17,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def header_functions():
     text = open(os.path.join(ROOT, "include", "tweakseq_gb300.h")).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return set(re.findall(r"^\s*(?:int|void)\s+\*?\s*(tsq_\w+)\s*\(", text, flags=re.M))
+    return set(re.findall(r"^\s*(?:int|void|size_t)\s+\*?\s*(tsq_\w+)\s*\(", text, flags=re.M))
 
 
 @pytest.fixture(scope="module")
@@ -53,3 +53,4 @@ def test_version_and_struct_layouts(lib):
     assert ctypes.sizeof(N.Params) == 40
     assert ctypes.sizeof(N.Result) == 48
     assert ctypes.sizeof(N.PairDesc) == 24
+    assert N.TREE_NODE_DTYPE.itemsize == 48

@@ -116,6 +116,12 @@ assert RESULT_DTYPE.itemsize == ctypes.sizeof(Result) and PAIR_DTYPE.itemsize ==
 _lib = None
 
 # Every function the header declares, with its ctypes signature.
+TREE_NODE_DTYPE = np.dtype([("left", np.int32), ("right", np.int32), ("size", np.int32), ("pos", np.int32),
+                            ("dist", np.int64), ("height", np.int64), ("left_length", np.int64),
+                            ("right_length", np.int64)])
+TREE = {"upgma": 0, "nj": 1}
+DIST_ONE = 1 << 32  # distances and branch lengths are in units of 2^-32
+
 _VP = ctypes.c_void_p
 _SIGS = {
     "tsq_version": ([ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_char_p)], ctypes.c_int),
@@ -145,6 +151,14 @@ _SIGS = {
     "tsq_probe_dpx": ([ctypes.c_int32, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     "tsq_align_score_noalloc": ([_VP, ctypes.c_int64, _VP, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(Params),
                                  _VP, _VP], ctypes.c_int),
+    "tsq_consensus": ([_VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.c_double, _VP, _VP, _VP],
+                      ctypes.c_int),
+    "tsq_consensus_scratch_bytes": ([ctypes.c_int32], ctypes.c_size_t),
+    "tsq_consensus_device": ([_VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.c_double, _VP, _VP, _VP,
+                              _VP, ctypes.c_size_t, _VP], ctypes.c_int),
+    "tsq_guide_tree_dist": ([ctypes.c_int32, _VP, ctypes.c_int32, _VP], ctypes.c_int),
+    "tsq_guide_tree": ([ctypes.c_int32, _VP, _VP, ctypes.c_int32, _VP], ctypes.c_int),
+    "tsq_batch_guide_tree": ([_VP, ctypes.c_int32, ctypes.c_int32, _VP], ctypes.c_int),
 }
 
 

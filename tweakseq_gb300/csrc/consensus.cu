@@ -1,0 +1,304 @@
+// consensus.cu -- consensus line of a gapped alignment on the GPU.
+//
+// Same result as Consensus::calculate (tweakseq/Core/Annotations/
+// Consensus.cpp:80-161), which for every column scores each row against
+// every other row (O(nseq^2) per column): +1 for two "gap" bytes (anything
+// outside 'A'..'Z', :96-106), -4 for one, BLOSUM62 otherwise; a pair counts as
+// a match when its score is positive.  The first row with the highest sum
+// wins, and the column shows that row's byte when its match count reaches
+// the plurality (default nseq / 2, :163-172), else '?'.
+//
+// A row's sum depends only on its class (23 BLOSUM62 rows + the gap class),
+// so the kernel counts classes per column and first row per class (one pass
+// over the bytes, HBM-bound), and the finishing kernel evaluates the 24
+// class sums from the counts: score(x) = sum_y count(y) S(x,y) - S(x,x).
+// All terms are integers, so this equals the reference's double sums
+// exactly; the first row with the best score is the smallest first-row index
+// among the best classes.
+#include <climits>
+#include <cstring>
+
+#include "engine.h"
+
+namespace tsq {
+namespace {
+
+constexpr int kClasses = 24;  // BLOSUM62 rows 0..22, 23 = gap class
+constexpr int kGapClass = 23;
+constexpr int kCountWarps = 8;
+constexpr int kCountThreads = kCountWarps * 32;
+constexpr int kTile = 128;  // columns per block
+
+__constant__ int8_t c_pair[kClasses][kClasses];  // class-vs-class pair scores
+__constant__ uint8_t c_class[256];                // byte -> class
+
+// A block covers 128 columns (lane t holds columns t, t+32, t+64, t+96 of
+// the tile, so that its counters fall in bank t) and one slice of the rows,
+// striped over its 8 warps.  With 4-byte-aligned rows a lane reads its 4
+// columns of a row with one 32-bit load.  Counts and first rows go to one
+// shared histogram per block (shared-memory atomics; the first-row minimum
+// is only attempted when the row can lower it), then into the column totals
+// with global atomics.
+template <bool kVec>
+__global__ void __launch_bounds__(kCountThreads) consensus_count_kernel(const uint8_t *__restrict__ rows, int32_t nseq,
+                                                                        int32_t ncols, int64_t stride,
+                                                                        int32_t rows_per_slice, uint32_t *cnt,
+                                                                        int32_t *first) {
+  __shared__ uint32_t h[kClasses][kTile];
+  __shared__ int32_t f[kClasses][kTile];
+  __shared__ uint8_t cls[256];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int k = threadIdx.x; k < kClasses * kTile; k += kCountThreads) {
+    (&h[0][0])[k] = 0u;
+    (&f[0][0])[k] = INT_MAX;
+  }
+  for (int k = threadIdx.x; k < 256; k += kCountThreads) cls[k] = c_class[k];
+  __syncthreads();
+  const int32_t c0 = blockIdx.x * kTile;
+  const int32_t r0 = blockIdx.y * rows_per_slice;
+  const int32_t r1 = min(nseq, r0 + rows_per_slice);
+  // This lane's columns: c0 + 4*lane .. +3 in memory, tile slots lane + 32u.
+  const int32_t mc = c0 + 4 * lane;
+  const int nvalid = max(0, min(4, ncols - mc));
+  if (nvalid > 0) {
+    const uint8_t *p = rows + mc;
+    auto load = [&](int32_t r) -> uint32_t {
+      if (kVec && nvalid == 4) return __ldg(reinterpret_cast<const uint32_t *>(p + int64_t(r) * stride));
+      uint32_t v = 0;
+      for (int u = 0; u < nvalid; ++u) v |= uint32_t(__ldg(p + int64_t(r) * stride + u)) << (8 * u);
+      return v;
+    };
+    auto count = [&](int32_t r, uint32_t v) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (u < nvalid) {
+          const int c = cls[(v >> (8 * u)) & 0xffu];
+          const int slot = lane + 32 * u;
+          atomicAdd(&h[c][slot], 1u);
+          if (r < f[c][slot]) atomicMin(&f[c][slot], r);
+        }
+      }
+    };
+    int32_t r = r0 + w;
+    // Four rows' loads in flight before their counts.
+    for (; r + 3 * kCountWarps < r1; r += 4 * kCountWarps) {
+      uint32_t v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = load(r + q * kCountWarps);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) count(r + q * kCountWarps, v[q]);
+    }
+    for (; r < r1; r += kCountWarps) count(r, load(r));
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < kClasses * kTile; e += kCountThreads) {
+    const int c = e / kTile, slot = e % kTile;
+    const uint32_t s = h[c][slot];
+    // Tile slot lane + 32u holds memory column c0 + 4*lane + u.
+    const int32_t col = c0 + 4 * (slot & 31) + (slot >> 5);
+    if (s != 0u && col < ncols) {
+      atomicAdd(&cnt[int64_t(col) * kClasses + c], s);
+      atomicMin(&first[int64_t(col) * kClasses + c], f[c][slot]);
+    }
+  }
+}
+
+__global__ void consensus_init_kernel(uint32_t *cnt, int32_t *first, int64_t n) {
+  for (int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; k < n; k += int64_t(gridDim.x) * blockDim.x) {
+    cnt[k] = 0u;
+    first[k] = INT_MAX;
+  }
+}
+
+// One thread per column: the 24 class sums from the counts.
+__global__ void consensus_finish_kernel(const uint8_t *__restrict__ rows, int32_t ncols, int64_t stride,
+                                        double plurality, const uint32_t *__restrict__ cnt,
+                                        const int32_t *__restrict__ first, uint8_t *out, int32_t *best_score,
+                                        int32_t *best_matches) {
+  const int32_t col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncols) return;
+  int64_t n[kClasses];
+#pragma unroll
+  for (int y = 0; y < kClasses; ++y) n[y] = cnt[int64_t(col) * kClasses + y];
+  int64_t bs = 0, bm = 0;
+  int32_t bf = INT_MAX;
+  bool have = false;
+#pragma unroll
+  for (int x = 0; x < kClasses; ++x) {
+    if (n[x] == 0) continue;
+    int64_t s = 0, mt = 0;
+#pragma unroll
+    for (int y = 0; y < kClasses; ++y) {
+      const int v = c_pair[x][y];
+      s += n[y] * v;
+      if (v > 0) mt += n[y];
+    }
+    // A row does not score against itself.
+    s -= c_pair[x][x];
+    if (c_pair[x][x] > 0) mt -= 1;
+    const int32_t fx = first[int64_t(col) * kClasses + x];
+    if (!have || s > bs || (s == bs && fx < bf)) {
+      have = true;
+      bs = s;
+      bm = mt;
+      bf = fx;
+    }
+  }
+  out[col] = double(bm) >= plurality ? rows[int64_t(bf) * stride + col] : uint8_t('?');
+  if (best_score) best_score[col] = int32_t(bs);
+  if (best_matches) best_matches[col] = int32_t(bm);
+}
+
+// BLOSUM62 row of each letter 'A'..'Z' (J, O, U, X share the X row), as the
+// reference's letter map; everything else is the gap class.
+void class_tables(int8_t pair[kClasses][kClasses], uint8_t cls[256]) {
+  static const char kOrder[23] = {'A', 'R', 'N', 'D', 'C', 'Q', 'E', 'G', 'H', 'I', 'L', 'K',
+                                  'M', 'F', 'P', 'S', 'T', 'W', 'Y', 'V', 'B', 'Z', 'X'};
+  for (int b = 0; b < 256; ++b) cls[b] = kGapClass;
+  for (int k = 0; k < 23; ++k) cls[uint8_t(kOrder[k])] = uint8_t(k);
+  cls[uint8_t('J')] = cls[uint8_t('O')] = cls[uint8_t('U')] = 22;
+  for (int x = 0; x < kClasses; ++x)
+    for (int y = 0; y < kClasses; ++y) {
+      if (x == kGapClass && y == kGapClass)
+        pair[x][y] = 1;
+      else if (x == kGapClass || y == kGapClass)
+        pair[x][y] = -4;
+      else
+        pair[x][y] = blosum62_by_row(x, y);
+    }
+}
+
+cudaError_t upload_tables() {
+  // The constant tables are per device; upload them once per device.
+  static thread_local int done_dev = -1;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || done_dev == dev) return e;
+  int8_t pair[kClasses][kClasses];
+  uint8_t cls[256];
+  class_tables(pair, cls);
+  e = cudaMemcpyToSymbol(c_pair, pair, sizeof(pair));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_class, cls, sizeof(cls));
+  if (e == cudaSuccess) done_dev = dev;
+  return e;
+}
+
+int sm_count() {
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
+int check_args(int32_t nseq, int32_t ncols, int64_t stride) {
+  if (nseq <= 0 || nseq > (1 << 27) || ncols < 0 || stride < ncols) return TSQ_E_INVALID_ARG;
+  return TSQ_OK;
+}
+
+// Launches on `stream`: counts, then the per-column decision.
+cudaError_t consensus_enqueue(const uint8_t *d_rows, int32_t nseq, int32_t ncols, int64_t stride, double plurality,
+                              uint8_t *d_out, int32_t *d_score, int32_t *d_matches, void *scratch,
+                              cudaStream_t stream) {
+  if (ncols == 0) return cudaSuccess;
+  cudaError_t e = upload_tables();
+  if (e != cudaSuccess) return e;
+  uint32_t *cnt = static_cast<uint32_t *>(scratch);
+  int32_t *first = reinterpret_cast<int32_t *>(cnt + int64_t(ncols) * kClasses);
+  const int64_t entries = int64_t(ncols) * kClasses;
+  consensus_init_kernel<<<int(std::min<int64_t>((entries + 255) / 256, 4096)), 256, 0, stream>>>(cnt, first,
+                                                                                                 entries);
+  // Enough blocks for every SM several times over: split the rows into
+  // slices when the columns alone do not give them.
+  const int32_t col_tiles = (ncols + kTile - 1) / kTile;
+  const int64_t want = int64_t(sm_count()) * 8;
+  int32_t slices = int32_t(std::max<int64_t>(1, std::min<int64_t>((want + col_tiles - 1) / col_tiles, 65535)));
+  int32_t per = (nseq + slices - 1) / slices;
+  per = std::max(per, 4 * kCountWarps);
+  slices = (nseq + per - 1) / per;
+  const bool vec = stride % 4 == 0 && reinterpret_cast<uintptr_t>(d_rows) % 4 == 0;
+  if (vec)
+    consensus_count_kernel<true><<<dim3(col_tiles, slices), kCountThreads, 0, stream>>>(d_rows, nseq, ncols, stride,
+                                                                                      per, cnt, first);
+  else
+    consensus_count_kernel<false><<<dim3(col_tiles, slices), kCountThreads, 0, stream>>>(d_rows, nseq, ncols, stride,
+                                                                                       per, cnt, first);
+  consensus_finish_kernel<<<(ncols + 127) / 128, 128, 0, stream>>>(d_rows, ncols, stride, plurality, cnt, first,
+                                                                   d_out, d_score, d_matches);
+  return cudaGetLastError();
+}
+
+struct ConsensusCache {
+  DevBuf rows, scratch, out;
+  cudaStream_t stream = nullptr;
+  int dev = -1;
+  ~ConsensusCache() {
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+}  // namespace
+
+size_t consensus_scratch_bytes(int32_t ncols) { return size_t(ncols > 0 ? ncols : 0) * kClasses * 8; }
+
+}  // namespace tsq
+
+extern "C" {
+
+size_t tsq_consensus_scratch_bytes(int32_t ncols) { return tsq::consensus_scratch_bytes(ncols); }
+
+int tsq_consensus_device(const uint8_t *d_rows, int32_t nseq, int32_t ncols, int64_t stride, double plurality,
+                         uint8_t *d_consensus, int32_t *d_best_score, int32_t *d_best_matches, void *d_scratch,
+                         size_t scratch_bytes, void *stream) {
+  if (int rc = tsq::check_args(nseq, ncols, stride)) return rc;
+  if (ncols > 0 && (!d_rows || !d_consensus || !d_scratch || scratch_bytes < tsq::consensus_scratch_bytes(ncols)))
+    return TSQ_E_INVALID_ARG;
+  if (plurality < 0) plurality = nseq / 2.0;
+  return tsq::cuda_status(tsq::consensus_enqueue(d_rows, nseq, ncols, stride, plurality, d_consensus, d_best_score,
+                                                 d_best_matches, d_scratch, static_cast<cudaStream_t>(stream)));
+}
+
+int tsq_consensus(const uint8_t *rows, int32_t nseq, int32_t ncols, int64_t stride, double plurality,
+                  uint8_t *consensus, int32_t *best_score, int32_t *best_matches) {
+  if (int rc = tsq::check_args(nseq, ncols, stride)) return rc;
+  if (ncols > 0 && (!rows || !consensus)) return TSQ_E_INVALID_ARG;
+  if (ncols == 0) return TSQ_OK;
+  if (plurality < 0) plurality = nseq / 2.0;
+  try {
+    thread_local tsq::ConsensusCache c;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return TSQ_E_CUDA;
+    if (c.dev != dev) {
+      c.rows.release();
+      c.scratch.release();
+      c.out.release();
+      if (c.stream) cudaStreamDestroy(c.stream);
+      c.stream = nullptr;
+      if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) return TSQ_E_CUDA;
+      c.dev = dev;
+    }
+    // Rows go up packed (pitch = ncols rounded up to 16 bytes).
+    const int64_t pitch = (int64_t(ncols) + 15) / 16 * 16;
+    cudaError_t e = c.rows.ensure(size_t(pitch) * size_t(nseq));
+    if (e == cudaSuccess) e = c.scratch.ensure(tsq::consensus_scratch_bytes(ncols));
+    if (e == cudaSuccess) e = c.out.ensure(size_t(ncols) * 9);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(c.rows.p, size_t(pitch), rows, size_t(stride), size_t(ncols), size_t(nseq),
+                            cudaMemcpyHostToDevice, c.stream);
+    uint8_t *d_out = c.out.as<uint8_t>();
+    int32_t *d_score = reinterpret_cast<int32_t *>(d_out + (int64_t(ncols) + 15) / 16 * 16);
+    int32_t *d_match = d_score + ncols;
+    if (e == cudaSuccess)
+      e = tsq::consensus_enqueue(c.rows.as<uint8_t>(), nseq, ncols, pitch, plurality, d_out, d_score, d_match,
+                                 c.scratch.p, c.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(consensus, d_out, size_t(ncols), cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess && best_score)
+      e = cudaMemcpyAsync(best_score, d_score, size_t(ncols) * 4, cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess && best_matches)
+      e = cudaMemcpyAsync(best_matches, d_match, size_t(ncols) * 4, cudaMemcpyDeviceToHost, c.stream);
+    const cudaError_t s = cudaStreamSynchronize(c.stream);
+    return tsq::cuda_status(e != cudaSuccess ? e : s);
+  } catch (const std::bad_alloc &) {
+    return TSQ_E_NOMEM;
+  }
+}
+
+}  // extern "C"

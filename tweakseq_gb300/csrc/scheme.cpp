@@ -43,6 +43,12 @@ constexpr int8_t kBlosum62[23][23] = {
 };
 // clang-format on
 
+}  // namespace
+
+int8_t blosum62_by_row(int x, int y) { return kBlosum62[x][y]; }
+
+namespace {
+
 int blosum_row(char letter) {
   if (letter == 'J' || letter == 'O' || letter == 'U') letter = 'X';
   const char *p = std::strchr(kRowOrder, letter);

@@ -103,6 +103,8 @@ struct WalkArgs {
 
 // Host-side helpers (scheme.cpp).
 int build_scheme(const tsq_params *p, Scheme *out);
+// BLOSUM62 entry by row index in the order ARNDCQEGHILKMFPSTWYVBZX.
+int8_t blosum62_by_row(int x, int y);
 void build_lut(const Scheme &s, uint8_t lut[256]);
 
 // Kernel launchers (fill_kernels.cu, walk_kernel.cu, encode in batch.cu).
