@@ -230,7 +230,9 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
       const int64_t go = p->gap_open, ge = p->gap_extend;
       const int64_t lowest = 3 * go + (int64_t(pd.a_len) + 512 + pd.b_len + 1) * ge + go + ge + 128 +
                              std::max<int64_t>(0, -int64_t(sc.min_score));
-      const bool lower_ok = lowest < 31000 && ge <= 700 && pd.b_len <= 65535;
+      // The int16x2 kernel also subtracts open + ext from values at this
+      // bound (T and XO), which must stay above -32768.
+      const bool lower_ok = lowest + go + ge < 31000 && ge <= 700 && pd.b_len <= 65535;
       const bool upper_ok =
           int64_t(std::max(sc.max_score, 0)) * std::min(pd.a_len, pd.b_len) + std::max(sc.max_score, 0) < 32767;
       if (lower_ok) lt = (upper_ok && p->lane == TSQ_LANE_AUTO) ? 1 : 2;

@@ -5,7 +5,9 @@
 namespace tsq {
 namespace fill {
 
-cudaError_t launch_i16(bool check, bool local, const FillArgs &a, int blocks, size_t smem, cudaStream_t st) {
+cudaError_t launch_i16(bool check, bool local, const FillArgs &args, int blocks, size_t smem, cudaStream_t st) {
+  FillArgs a = args;
+  a.one = 1u;
   if (check) {
     if (local)
       fill_i16_kernel<true, true><<<blocks, kThreads16, smem, st>>>(a);

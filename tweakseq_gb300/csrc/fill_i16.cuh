@@ -13,13 +13,22 @@
 // band B goes back to HBM.
 //
 // Per packed cell the fill issues 7 instructions: the profile PRMT that
-// builds the two int16 scores and six DPX add/max forms -- E = max(E - ext,
-// T), X = max(D + s, E), F = max(F_above - ext, XO_above), H = max(X, F),
-// T = H - (open + ext) for the next column's E, and XO = X - (open + ext)
-// (X clamped at 0 first in local mode) for the next row's F.  F can take X
-// instead of H from the row above because open >= 0 makes the F - open - ext
-// candidate redundant, so rows depend on each other through one add-max
-// only.
+// builds the two int16 scores, four DPX add/max forms -- E = max(E - ext,
+// T), X = max(D + s, E), F = max(F_above - ext, XO_above), H = max(X, F) --
+// and two subtractions, T = H - (open + ext) for the next column's E and
+// XO = X - (open + ext) (X clamped at 0 first in local mode) for the next
+// row's F.  F can take X instead of H from the row above because open >= 0
+// makes the F - open - ext candidate redundant, so rows depend on each other
+// through one add-max only.
+//
+// Biased halves.  Every value v is held as v + 32768 in an unsigned 16-bit
+// half, compared with the unsigned DPX forms; the proven range keeps every
+// half inside [0, 65535] and every subtrahend below it, so a packed
+// subtraction is one plain 32-bit subtraction (no borrow crosses the
+// halves).  Those two subtractions are issued as integer multiply-adds,
+// which run on the FMA pipe beside the DPX instructions' ALU pipe (the
+// kernel is ALU-pipe bound).  Adds of signed amounts (scores, -ext) stay in
+// the DPX add-max forms, whose per-half addition is modulo 2^16.
 //
 // Range.  The planner only sends a pair here when every value of its matrix
 // fits int16: H <= max_score * min(m, n) and every H, E, F >= -(3*open +
@@ -41,10 +50,25 @@ constexpr int kThreads16 = 128;  // 4 warps per block: the profile is 416 bytes 
 constexpr int kSlots16 = kThreads16 / 32 * 8;
 constexpr int kCodeRing16 = 256;  // band B reads codes up to 2G columns behind band A
 constexpr int32_t kNeg16 = -32000;
-constexpr uint32_t kNeg2 = 0x83008300u;  // kNeg16 in both halves
+constexpr int32_t kBias16 = 32768;
+constexpr uint32_t kBias2 = 0x80008000u;  // value 0 in both (biased) halves
+constexpr uint32_t kNeg2 = 0x03000300u;   // kNeg16 in both (biased) halves
 
 __device__ __forceinline__ uint32_t pack2(int32_t lo, int32_t hi) {
   return (uint32_t(lo) & 0xFFFFu) | (uint32_t(hi) << 16);
+}
+
+// Values as biased halves.
+__device__ __forceinline__ uint32_t pack2b(int32_t lo, int32_t hi) { return pack2(lo + kBias16, hi + kBias16); }
+__device__ __forceinline__ int32_t lo16b(uint32_t v) { return int32_t(v & 0xFFFFu) - kBias16; }
+__device__ __forceinline__ int32_t hi16b(uint32_t v) { return int32_t(v >> 16) - kBias16; }
+
+// a - sub2 for biased packed halves (each half of a >= its subtrahend),
+// issued as an integer multiply-add by the opaque 1.
+__device__ __forceinline__ uint32_t sub2_imad(uint32_t a, uint32_t one, uint32_t neg_sub2) {
+  uint32_t d;
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(one), "r"(neg_sub2));
+  return d;
 }
 
 // (sign-extended byte K of a, sign-extended byte K of b) as int16x2.
@@ -89,6 +113,9 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
   const int gw = lane >> lg;
   const int32_t go = A.gap_open, ge = A.gap_extend, oe = go + ge;
   const uint32_t nge2 = pack2(-ge, -ge), noe2 = pack2(-oe, -oe);
+  const uint32_t one = A.one;
+  const uint32_t neg_oe2 = 0u - ((uint32_t(oe) << 16) | uint32_t(oe));  // adds -(oe, oe) without borrows
+  const uint32_t zero_oe2 = pack2b(-oe, -oe);                          // max(x, 0) - oe floor, local
   uint32_t *top = reinterpret_cast<uint32_t *>(A.bnd) + ((int64_t)warp_id * 8 + gw) * A.bnd_cols;
   const int gslot = (threadIdx.x >> 5) * 8 + gw;
   constexpr int kTopStride = kTopRing * 4 + kRingPad;  // bytes
@@ -128,12 +155,12 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
 
   // Row 0 of the matrix becomes the first top row: (H, F) as int16 halves.
   if (!trivial)
-    for (int j = t; j < n; j += G) top[j] = pack2(edge_h(j + 1, go, ge, LOCAL), kNeg16);
+    for (int j = t; j < n; j += G) top[j] = pack2b(edge_h(j + 1, go, ge, LOCAL), kNeg16);
   __syncwarp();
 
   int32_t lbest = 0, lrow = 0, lcol = 0;
   int32_t last_h = 0;
-  uint32_t hmax = LOCAL ? 0u : kNeg2;
+  uint32_t hmax = LOCAL ? kBias2 : kNeg2;
 
   for (int pass = 0; pass < max_passes; ++pass) {
     const bool gact = pass < passes;
@@ -172,14 +199,14 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
     uint32_t best[R], bcol[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      H[r] = pack2(edge_h(rowA + r + 1, go, ge, LOCAL), edge_h(rowB + r + 1, go, ge, LOCAL));
-      T[r] = __viaddmax_s16x2(H[r], noe2, kNeg2);
+      H[r] = pack2b(edge_h(rowA + r + 1, go, ge, LOCAL), edge_h(rowB + r + 1, go, ge, LOCAL));
+      T[r] = __viaddmax_u16x2(H[r], noe2, kNeg2);
       E[r] = kNeg2;
-      best[r] = 0u;
+      best[r] = kBias2;
       bcol[r] = 0u;
     }
-    uint32_t hdiag = pack2(edge_h(rowA, go, ge, LOCAL), edge_h(rowB, go, ge, LOCAL));
-    uint32_t outH = 0u, outF = kNeg2;
+    uint32_t hdiag = pack2b(edge_h(rowA, go, ge, LOCAL), edge_h(rowB, go, ge, LOCAL));
+    uint32_t outH = kBias2, outF = kNeg2;
 
     cp_async_wait_all();
     __syncwarp();
@@ -238,7 +265,7 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
             uint32_t d = hdiag;
             hdiag = keep ? ((upH & ~keep) | (hdiag & keep)) : upH;
             // F of the lane's first row from the row above it.
-            uint32_t fv = __viaddmax_s16x2(upF, nge2, __viaddmax_s16x2(upH, noe2, kNeg2));
+            uint32_t fv = __viaddmax_u16x2(upF, nge2, __viaddmax_u16x2(upH, noe2, kNeg2));
             uint32_t xo = 0u;
             // Rows in order.  Since open >= 0, F(i+1,j) = max(F(i,j) - ext,
             // max(X(i,j) [, 0]) - open - ext) with X = max(D + s, E): the
@@ -248,23 +275,23 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
 #pragma unroll
               for (int r = 0; r < R; ++r) {
                 const uint32_t sc = score2_dyn(r < 4 ? wa.x : wa.y, r < 4 ? wb.x : wb.y, r);
-                uint32_t e = __viaddmax_s16x2(E[r], nge2, T[r]);
-                const uint32_t x = __viaddmax_s16x2(d, sc, e);
-                const uint32_t f = r == 0 ? fv : __viaddmax_s16x2(fv, nge2, xo);
-                uint32_t h = LOCAL ? __vimax_s16x2_relu(x, f) : __vimax3_s16x2(x, f, f);
-                uint32_t tn = __viaddmax_s16x2(h, noe2, kNeg2);
-                xo = LOCAL ? __viaddmax_s16x2(x, noe2, noe2) : __viaddmax_s16x2(x, noe2, kNeg2);
+                uint32_t e = __viaddmax_u16x2(E[r], nge2, T[r]);
+                const uint32_t x = __viaddmax_u16x2(d, sc, e);
+                const uint32_t f = r == 0 ? fv : __viaddmax_u16x2(fv, nge2, xo);
+                uint32_t h = LOCAL ? __vimax3_u16x2(x, f, kBias2) : __vimax3_u16x2(x, f, f);
+                uint32_t tn = sub2_imad(h, one, neg_oe2);
+                xo = LOCAL ? __viaddmax_u16x2(x, noe2, zero_oe2) : sub2_imad(x, one, neg_oe2);
                 if constexpr (MASKED) {
                   h = (h & ~keep) | (H[r] & keep);
                   tn = (tn & ~keep) | (T[r] & keep);
                   e = (e & ~keep) | (E[r] & keep);
                 }
-                if constexpr (CHECK) hmax = __vimax3_s16x2(hmax, h, h);
+                if constexpr (CHECK) hmax = __vimax3_u16x2(hmax, h, h);
                 if constexpr (LOCAL) {
                   // Halves where this cell beats the row's best so far
                   // (strictly, so the first column of a maximum is kept).
-                  const uint32_t cm = __vcmpgts2(h, best[r]);
-                  best[r] = __vimax3_s16x2(best[r], h, h);
+                  const uint32_t cm = __vcmpgtu2(h, best[r]);
+                  best[r] = __vimax3_u16x2(best[r], h, h);
                   bcol[r] = (bcol[r] & ~cm) | (pack2(jA + 1, jB + 1) & cm);
                 }
                 d = H[r];
@@ -297,7 +324,7 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
 #pragma unroll
           for (int r = 0; r < R; ++r) {
             const int row = (half ? rowB : rowA) + r;
-            const int32_t v = half ? int32_t(int16_t(best[r] >> 16)) : int32_t(int16_t(best[r] & 0xFFFFu));
+            const int32_t v = half ? hi16b(best[r]) : lo16b(best[r]);
             const int32_t c = half ? int32_t(bcol[r] >> 16) : int32_t(bcol[r] & 0xFFFFu);
             if (row < m && v > lbest) {
               lbest = v;
@@ -312,7 +339,7 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
         const int lr = (w - half * P) - t * R;
 #pragma unroll
         for (int r = 0; r < R; ++r)
-          if (r == lr) last_h = half ? int32_t(int16_t(H[r] >> 16)) : int32_t(int16_t(H[r] & 0xFFFFu));
+          if (r == lr) last_h = half ? hi16b(H[r]) : lo16b(H[r]);
       }
     }
   }
@@ -321,7 +348,7 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
   bool overflow = false;
   if constexpr (CHECK) {
     const int32_t lim = 32767 - A.max_score;
-    overflow = int32_t(int16_t(hmax & 0xFFFFu)) > lim || int32_t(int16_t(hmax >> 16)) > lim;
+    overflow = lo16b(hmax) > lim || hi16b(hmax) > lim;
   }
   const bool goverflow = (__ballot_sync(0xffffffffu, overflow) & gm) != 0;
   if constexpr (LOCAL) {

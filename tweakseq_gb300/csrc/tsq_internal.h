@@ -77,6 +77,7 @@ struct FillArgs {
   const int64_t *plane_off;  // byte offset of each pair's planes
   int32_t *overflow;     // int16 CHECK: per pair, 1 when a lane came near 32767
   int32_t max_score;     // largest substitution score of the scheme
+  uint32_t one;          // int16x2 fill: 1, an opaque multiplier for packed subtractions on the IMAD pipe
 };
 
 // Compacts the pairs an int16 CHECK launch flagged into a warp-task list
