@@ -227,88 +227,92 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       tv[0] = top_ring[0];
     }
 
-    for (int s0 = 0; s0 < max_steps; s0 += 2) {
+    // Steps run in pairs; an odd count gets one padding step, in which every
+    // lane's columns are out of range (s - t >= n + G).
+    const int steps_pad = (max_steps + 1) & ~1;
+    for (int s0 = 0; s0 < steps_pad; s0 += 2) {
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
         const int s = s0 + k;
-        if (s < max_steps) {
-          if (((s + 1) & (kChunk - 1)) == 0) {
-            cp_async_wait_all();
-            __syncwarp();
-            stage_chunk_rt<uint32_t, kCodeRing16>(G, (s + 1) / kChunk + 1, t, nact, top, top_ring, A.codes, boff,
-                                                  code_ring);
-            cp_async_commit();
-          }
-          const uint32_t rH = __shfl_sync(0xffffffffu, outH, src_lane);
-          const uint32_t rF = __shfl_sync(0xffffffffu, outF, src_lane);
-          const int jA = s - t, jB = jA - G;
-          const bool vA = (unsigned)jA < (unsigned)nact;
-          const bool vB = (unsigned)jB < (unsigned)nact;
-          const uint2 wa = pa[k & 1], wb = pb[k & 1];
-          {
-            const int ca = min(int(code_ring[(boff + jA + 1) & (kCodeRing16 - 1)]), kLetters - 1);
-            const int cb = min(int(code_ring[(boff + jB + 1) & (kCodeRing16 - 1)]), kLetters - 1);
-            pa[(k + 1) & 1] = profA[(2 * ca) * kThreads16];
-            pb[(k + 1) & 1] = profB[(2 * cb) * kThreads16];
-          }
-          uint32_t upH = rH, upF = rF;
-          if (t == 0) {
-            // Band A: the staged top row; band B: lane G-1's band-A bottom.
-            upH = prmt(tv[k & 1], rH, 0x5410u);
-            upF = prmt(tv[k & 1], rF, 0x5432u);
-            tv[(k + 1) & 1] = top_ring[(jA + 1) & (kTopRing - 1)];
-          }
-          if (vA || vB) {
-            // Halves outside their column range keep their old values.
-            const uint32_t keep = (vA ? 0u : 0x0000FFFFu) | (vB ? 0u : 0xFFFF0000u);
-            // A half that has not started keeps its left-boundary diagonal.
-            uint32_t d = hdiag;
-            hdiag = keep ? ((upH & ~keep) | (hdiag & keep)) : upH;
-            // F of the lane's first row from the row above it.
-            uint32_t fv = __viaddmax_u16x2(upF, nge2, __viaddmax_u16x2(upH, noe2, kNeg2));
-            uint32_t xo = 0u;
-            // Rows in order.  Since open >= 0, F(i+1,j) = max(F(i,j) - ext,
-            // max(X(i,j) [, 0]) - open - ext) with X = max(D + s, E): the
-            // only dependence between rows is one add-max on F.
-            auto sweep = [&](auto masked_tag) {
-              constexpr bool MASKED = decltype(masked_tag)::value;
+        // Chunk boundaries fall on odd steps only (s0 is even).
+        if (k == 1 && ((s + 1) & (kChunk - 1)) == 0) {
+          cp_async_wait_all();
+          __syncwarp();
+          stage_chunk_rt<uint32_t, kCodeRing16>(G, (s + 1) / kChunk + 1, t, nact, top, top_ring, A.codes, boff,
+                                                code_ring);
+          cp_async_commit();
+        }
+        const uint32_t rH = __shfl_sync(0xffffffffu, outH, src_lane);
+        const uint32_t rF = __shfl_sync(0xffffffffu, outF, src_lane);
+        const int jA = s - t, jB = jA - G;
+        const bool vA = (unsigned)jA < (unsigned)nact;
+        const bool vB = (unsigned)jB < (unsigned)nact;
+        const uint2 wa = pa[k & 1], wb = pb[k & 1];
+        {
+          const int ca = min(int(code_ring[(boff + jA + 1) & (kCodeRing16 - 1)]), kLetters - 1);
+          const int cb = min(int(code_ring[(boff + jB + 1) & (kCodeRing16 - 1)]), kLetters - 1);
+          pa[(k + 1) & 1] = profA[(2 * ca) * kThreads16];
+          pb[(k + 1) & 1] = profB[(2 * cb) * kThreads16];
+        }
+        uint32_t upH = rH, upF = rF;
+        if (t == 0) {
+          // Band A: the staged top row; band B: lane G-1's band-A bottom.
+          upH = prmt(tv[k & 1], rH, 0x5410u);
+          upF = prmt(tv[k & 1], rF, 0x5432u);
+          tv[(k + 1) & 1] = top_ring[(jA + 1) & (kTopRing - 1)];
+        }
+        if (vA || vB) {
+          uint32_t d = hdiag;
+          // F of the lane's first row from the row above it.
+          uint32_t fv = __viaddmax_u16x2(upF, nge2, __viaddmax_u16x2(upH, noe2, kNeg2));
+          uint32_t xo = 0u;
+          // Rows in order.  Since open >= 0, F(i+1,j) = max(F(i,j) - ext,
+          // max(X(i,j) [, 0]) - open - ext) with X = max(D + s, E): the
+          // only dependence between rows is one add-max on F.
+          auto sweep = [&](auto masked_tag, uint32_t keep) {
+            constexpr bool MASKED = decltype(masked_tag)::value;
 #pragma unroll
-              for (int r = 0; r < R; ++r) {
-                const uint32_t sc = score2_dyn(r < 4 ? wa.x : wa.y, r < 4 ? wb.x : wb.y, r);
-                uint32_t e = __viaddmax_u16x2(E[r], nge2, T[r]);
-                const uint32_t x = __viaddmax_u16x2(d, sc, e);
-                const uint32_t f = r == 0 ? fv : __viaddmax_u16x2(fv, nge2, xo);
-                uint32_t h = LOCAL ? __vimax3_u16x2(x, f, kBias2) : __vimax3_u16x2(x, f, f);
-                uint32_t tn = sub2_imad(h, one, neg_oe2);
-                xo = LOCAL ? __viaddmax_u16x2(x, noe2, zero_oe2) : sub2_imad(x, one, neg_oe2);
-                if constexpr (MASKED) {
-                  h = (h & ~keep) | (H[r] & keep);
-                  tn = (tn & ~keep) | (T[r] & keep);
-                  e = (e & ~keep) | (E[r] & keep);
-                }
-                if constexpr (CHECK) hmax = __vimax3_u16x2(hmax, h, h);
-                if constexpr (LOCAL) {
-                  // Halves where this cell beats the row's best so far
-                  // (strictly, so the first column of a maximum is kept).
-                  const uint32_t cm = __vcmpgtu2(h, best[r]);
-                  best[r] = __vimax3_u16x2(best[r], h, h);
-                  bcol[r] = (bcol[r] & ~cm) | (pack2(jA + 1, jB + 1) & cm);
-                }
-                d = H[r];
-                H[r] = h;
-                T[r] = tn;
-                E[r] = e;
-                fv = f;
+            for (int r = 0; r < R; ++r) {
+              const uint32_t sc = score2_dyn(r < 4 ? wa.x : wa.y, r < 4 ? wb.x : wb.y, r);
+              uint32_t e = __viaddmax_u16x2(E[r], nge2, T[r]);
+              const uint32_t x = __viaddmax_u16x2(d, sc, e);
+              const uint32_t f = r == 0 ? fv : __viaddmax_u16x2(fv, nge2, xo);
+              uint32_t h = LOCAL ? __vimax3_u16x2(x, f, kBias2) : __vimax3_u16x2(x, f, f);
+              uint32_t tn = sub2_imad(h, one, neg_oe2);
+              xo = LOCAL ? __viaddmax_u16x2(x, noe2, zero_oe2) : sub2_imad(x, one, neg_oe2);
+              if constexpr (MASKED) {
+                h = (h & ~keep) | (H[r] & keep);
+                tn = (tn & ~keep) | (T[r] & keep);
+                e = (e & ~keep) | (E[r] & keep);
               }
-            };
-            if (keep == 0u)
-              sweep(BoolTag<false>{});
-            else
-              sweep(BoolTag<true>{});
-            outH = H[R - 1];
-            outF = fv;
-            if (t == G - 1 && vB) top[jB] = prmt(outH, outF, 0x7632u);
+              if constexpr (CHECK) hmax = __vimax3_u16x2(hmax, h, h);
+              if constexpr (LOCAL) {
+                // Halves where this cell beats the row's best so far
+                // (strictly, so the first column of a maximum is kept).
+                const uint32_t cm = __vcmpgtu2(h, best[r]);
+                best[r] = __vimax3_u16x2(best[r], h, h);
+                bcol[r] = (bcol[r] & ~cm) | (pack2(jA + 1, jB + 1) & cm);
+              }
+              d = H[r];
+              H[r] = h;
+              T[r] = tn;
+              E[r] = e;
+              fv = f;
+            }
+          };
+          if (vA && vB) {
+            hdiag = upH;
+            sweep(BoolTag<false>{}, 0u);
+          } else {
+            // Halves outside their column range keep their old values; a
+            // half that has not started keeps its left-boundary diagonal.
+            const uint32_t keep = vA ? 0xFFFF0000u : 0x0000FFFFu;
+            hdiag = (upH & ~keep) | (hdiag & keep);
+            sweep(BoolTag<true>{}, keep);
           }
+          outH = H[R - 1];
+          outF = fv;
+          if (t == G - 1 && vB) top[jB] = prmt(outH, outF, 0x7632u);
         }
       }
     }
