@@ -1,6 +1,7 @@
 """GPU parity: the CUDA library, called through its C ABI, against the CPU
 oracle on the same seeded inputs.  Integer work, so the bar is bit-exact:
 scores, coordinates, identity counts and both gapped strings."""
+import ctypes
 import json
 import os
 
@@ -294,3 +295,39 @@ def test_long_pairs_on_the_cta_fill_all_outputs(local):
     a, b = ps.pair(2)
     r = A.align_pair(a, b, matrix="dna", gap_open=5, gap_extend=2, mode="local" if local else "global")
     assert (r.score, r.aln_a, r.aln_b) == (int(want["score"][2]), sa[2], sb[2])
+
+
+def test_alignment_batch_in_waves(monkeypatch):
+    """An alignment batch whose traceback planes exceed the memory budget
+    runs in waves (largest pairs first); every result matches the
+    single-wave run and the oracle."""
+    rng = np.random.default_rng(31)
+    seqs, pairs = [], []
+    for k in range(24):
+        a = W.DNA_LETTERS[rng.integers(0, 4, int(rng.integers(200, 3000)))]
+        seqs += [a.tobytes(), W._mutate_dna(rng, a, 0.1, 0.02, 3.0).tobytes()]
+        pairs.append((2 * k, 2 * k + 1))
+    ps = W._pairset_from_lists(seqs, pairs, matrix=W.DNA, gap_open=5, gap_extend=2)
+    kw = dict(matrix="dna", gap_open=5, gap_extend=2, output="alignment")
+    whole = A.align_batch(ps, **kw)
+    monkeypatch.setenv("TSQ_WAVE_BUDGET_BYTES", str(12 << 20))  # a few pairs per wave
+    waved = A.align_batch(ps, **kw)
+    for f in ("score", "a_begin", "a_end", "b_begin", "b_end", "n_ident", "n_cols", "status"):
+        assert np.array_equal(whole.table[f], waved.table[f]), f
+    assert whole.aln_a == waved.aln_a and whole.aln_b == waved.aln_b
+    want, sa, sb = O.batch(ps.seqs, ps.a_off, ps.a_len, ps.b_off, ps.b_len, O.DNA, 5, 2, False, O.MODE_ALIGN, 0, True)
+    assert waved.aln_a == sa and waved.aln_b == sb
+    assert np.array_equal(waved.table["score"], want["score"])
+    # A pair larger than the budget on its own is refused, the rest align.
+    monkeypatch.setenv("TSQ_WAVE_BUDGET_BYTES", str(1 << 20))
+    raw = np.zeros(len(ps), dtype=N.RESULT_DTYPE)
+    seqs_arr, tab = A._as_inputs(ps)
+    p, keep = N.make_params(**kw)
+    rc = N.lib().tsq_align_batch(seqs_arr.ctypes.data, len(seqs_arr), tab.ctypes.data, len(tab), ctypes.byref(p),
+                                 ctypes.byref(A._opts()), raw.ctypes.data)
+    assert rc == N.E_TOO_LARGE
+    a_len, b_len = ps.a_len.astype(np.int64), ps.b_len.astype(np.int64)
+    big = (a_len + 255) * (b_len + 31) // 2 + 2 * (a_len + b_len) + 512 > (1 << 20)
+    assert big.any() and (~big).any()
+    assert np.all(raw["status"][big] == N.E_TOO_LARGE) and np.all(raw["status"][~big] == 0)
+    N.lib().tsq_results_free(raw.ctypes.data, len(raw))

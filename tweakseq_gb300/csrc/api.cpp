@@ -1,9 +1,11 @@
 // api.cpp -- the extern "C" entry points declared in include/tweakseq_gb300.h.
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <exception>
 #include <memory>
 #include <new>
+#include <vector>
 
 #include "engine.h"
 
@@ -40,6 +42,51 @@ int guarded(F &&f) {
   } catch (...) {
     return TSQ_E_CUDA;
   }
+}
+
+// Runs an alignment batch wave by wave (see tsq_align_batch).
+int align_in_waves(tsq_batch *e, const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *pairs, int64_t n,
+                   const tsq_params *p, const tsq_batch_opts *opts, tsq_result *out,
+                   const std::vector<int64_t> &bytes, int64_t budget) {
+  std::vector<int64_t> order(static_cast<size_t>(n));
+  for (int64_t k = 0; k < n; ++k) order[size_t(k)] = k;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int64_t x, int64_t y) { return bytes[size_t(x)] > bytes[size_t(y)]; });
+  std::memset(out, 0, sizeof(tsq_result) * size_t(n));
+  std::vector<tsq_pair_desc> wave;
+  std::vector<tsq_result> res;
+  int status = TSQ_OK;
+  int64_t begin = 0;
+  while (begin < n) {
+    int64_t end = begin, used = 0;
+    while (end < n && (end == begin || used + bytes[size_t(order[size_t(end)])] <= budget))
+      used += bytes[size_t(order[size_t(end++)])];
+    if (used > budget) {  // one pair alone is larger than the budget
+      for (int64_t k = begin; k < end; ++k) out[order[size_t(k)]].status = TSQ_E_TOO_LARGE;
+      status = status ? status : TSQ_E_TOO_LARGE;
+      begin = end;
+      continue;
+    }
+    wave.resize(size_t(end - begin));
+    res.assign(size_t(end - begin), tsq_result{});
+    for (int64_t k = begin; k < end; ++k) wave[size_t(k - begin)] = pairs[order[size_t(k)]];
+    int rc = tsq::batch_plan(e, seqs, seqs_len, wave.data(), end - begin, p, opts, false);
+    if (rc == TSQ_OK) rc = tsq::batch_run_async(e);
+    if (rc == TSQ_OK) rc = tsq::batch_sync(e);
+    if (rc == TSQ_OK || rc == TSQ_E_INVALID_RESIDUE) {
+      const int rr = tsq::batch_results(e, res.data());
+      rc = rc ? rc : rr;
+    }
+    if (rc != TSQ_OK && rc != TSQ_E_INVALID_RESIDUE) {
+      tsq_results_free(res.data(), int64_t(res.size()));
+      tsq_results_free(out, n);
+      return rc;
+    }
+    if (rc) status = status ? status : rc;
+    for (int64_t k = begin; k < end; ++k) out[order[size_t(k)]] = res[size_t(k - begin)];  // strings move over
+    begin = end;
+  }
+  return status;
 }
 
 }  // namespace
@@ -102,6 +149,32 @@ int tsq_align_batch(const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *
       c.batch_dev = dev;
     }
     tsq_batch *e = c.batch_engine.get();
+    if (p && p->output == TSQ_OUT_ALIGNMENT && n > 1 && pairs) {
+      // Traceback planes take about m*n/2 bytes per pair.  A batch whose
+      // planes do not fit in the device memory that is free runs in waves:
+      // pairs by plane size, largest first (so that the pairs of a wave are
+      // alike and no wave waits on one long pair), each wave as many pairs as
+      // fit in 60 % of the free memory.  Results land at the pairs' own
+      // positions; a pair too large for any wave is TSQ_E_TOO_LARGE.
+      if (cudaSetDevice(dev) != cudaSuccess) return TSQ_E_CUDA;
+      size_t free_b = 0, total_b = 0;
+      if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return TSQ_E_CUDA;
+      int64_t budget = int64_t(0.6 * double(free_b + e->planes.cap + e->aln.cap));
+      // TSQ_WAVE_BUDGET_BYTES lowers the budget (tests use it to force waves).
+      if (const char *env = std::getenv("TSQ_WAVE_BUDGET_BYTES")) {
+        const long long v = std::atoll(env);
+        if (v > 0) budget = std::min<int64_t>(budget, v);
+      }
+      std::vector<int64_t> bytes(static_cast<size_t>(n));
+      int64_t total = 0;
+      for (int64_t k = 0; k < n; ++k) {
+        const tsq_pair_desc &d = pairs[k];
+        bytes[size_t(k)] = (std::max<int64_t>(d.a_len, 0) + 255) * (std::max<int64_t>(d.b_len, 0) + 31) / 2 +
+                           2 * (int64_t(std::max(d.a_len, 0)) + std::max(d.b_len, 0)) + 512;
+        total += bytes[size_t(k)];
+      }
+      if (total > budget) return align_in_waves(e, seqs, seqs_len, pairs, n, p, opts, out, bytes, budget);
+    }
     int rc = tsq::batch_plan(e, seqs, seqs_len, pairs, n, p, opts, false);
     if (rc) return rc;
     if ((rc = tsq::batch_run_async(e))) return rc;

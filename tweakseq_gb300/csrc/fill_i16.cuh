@@ -124,6 +124,8 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
   const uint2 *profA = s_prof + threadIdx.x;                // + (2c) * kThreads16
   const uint2 *profB = s_prof + kThreads16 + threadIdx.x;   // + (2c) * kThreads16
   const int src_lane = (lane & ~(G - 1)) | ((t + G - 1) & (G - 1));  // rotate within the group
+  const uint32_t selH = t == 0 ? 0x5410u : 0x7654u;  // (top H, rotated band-A H) or the shuffled word
+  const uint32_t selF = t == 0 ? 0x5432u : 0x7654u;
 
   const bool have = gw < count;
   const int pid = have ? A.tasks[begin + gw] : 0;
@@ -254,13 +256,13 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
           pa[(k + 1) & 1] = profA[(2 * ca) * kThreads16];
           pb[(k + 1) & 1] = profB[(2 * cb) * kThreads16];
         }
-        uint32_t upH = rH, upF = rF;
-        if (t == 0) {
-          // Band A: the staged top row; band B: lane G-1's band-A bottom.
-          upH = prmt(tv[k & 1], rH, 0x5410u);
-          upF = prmt(tv[k & 1], rF, 0x5432u);
-          tv[(k + 1) & 1] = top_ring[(jA + 1) & (kTopRing - 1)];
-        }
+        // Lane 0: band A from the staged top row, band B from lane G-1's
+        // band-A bottom; other lanes take the shuffled values whole.  Lane-
+        // dependent PRMT selectors instead of a branch; every lane of a group
+        // reads lane 0's ring entry (one broadcast address per group).
+        const uint32_t upH = prmt(tv[k & 1], rH, selH);
+        const uint32_t upF = prmt(tv[k & 1], rF, selF);
+        tv[(k + 1) & 1] = top_ring[(s + 1) & (kTopRing - 1)];
         if (vA || vB) {
           uint32_t d = hdiag;
           // F of the lane's first row from the row above it.
