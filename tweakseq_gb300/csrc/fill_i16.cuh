@@ -98,6 +98,10 @@ template <bool B>
 struct BoolTag {
   static constexpr bool value = B;
 };
+template <int K>
+struct IntTag {
+  static constexpr int value = K;
+};
 
 // The lane width G is a run-time value: one code path serves every width,
 // which keeps the kernel small enough for the instruction cache.
@@ -230,93 +234,113 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
     }
 
     // Steps run in pairs; an odd count gets one padding step, in which every
-    // lane's columns are out of range (s - t >= n + G).
+    // lane's columns are out of range (s - t >= n + G).  Steps [2G, n_min)
+    // -- n_min the shortest column count of the warp's groups this pass,
+    // 0 when one of them is idle -- have both halves of every lane in range:
+    // they run without range tests or masks.
     const int steps_pad = (max_steps + 1) & ~1;
-    for (int s0 = 0; s0 < steps_pad; s0 += 2) {
+    int n_min = nact;
 #pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int s = s0 + k;
-        // Chunk boundaries fall on odd steps only (s0 is even).
-        if (k == 1 && ((s + 1) & (kChunk - 1)) == 0) {
-          cp_async_wait_all();
-          __syncwarp();
-          stage_chunk_rt<uint32_t, kCodeRing16>(G, (s + 1) / kChunk + 1, t, nact, top, top_ring, A.codes, boff,
-                                                code_ring);
-          cp_async_commit();
-        }
-        const uint32_t rH = __shfl_sync(0xffffffffu, outH, src_lane);
-        const uint32_t rF = __shfl_sync(0xffffffffu, outF, src_lane);
-        const int jA = s - t, jB = jA - G;
-        const bool vA = (unsigned)jA < (unsigned)nact;
-        const bool vB = (unsigned)jB < (unsigned)nact;
-        const uint2 wa = pa[k & 1], wb = pb[k & 1];
-        {
-          const int ca = min(int(code_ring[(boff + jA + 1) & (kCodeRing16 - 1)]), kLetters - 1);
-          const int cb = min(int(code_ring[(boff + jB + 1) & (kCodeRing16 - 1)]), kLetters - 1);
-          pa[(k + 1) & 1] = profA[(2 * ca) * kThreads16];
-          pb[(k + 1) & 1] = profB[(2 * cb) * kThreads16];
-        }
-        // Lane 0: band A from the staged top row, band B from lane G-1's
-        // band-A bottom; other lanes take the shuffled values whole.  Lane-
-        // dependent PRMT selectors instead of a branch; every lane of a group
-        // reads lane 0's ring entry (one broadcast address per group).
-        const uint32_t upH = prmt(tv[k & 1], rH, selH);
-        const uint32_t upF = prmt(tv[k & 1], rF, selF);
-        tv[(k + 1) & 1] = top_ring[(s + 1) & (kTopRing - 1)];
-        if (vA || vB) {
-          uint32_t d = hdiag;
-          // F of the lane's first row from the row above it.
-          uint32_t fv = __viaddmax_u16x2(upF, nge2, __viaddmax_u16x2(upH, noe2, kNeg2));
-          uint32_t xo = 0u;
-          // Rows in order.  Since open >= 0, F(i+1,j) = max(F(i,j) - ext,
-          // max(X(i,j) [, 0]) - open - ext) with X = max(D + s, E): the
-          // only dependence between rows is one add-max on F.
-          auto sweep = [&](auto masked_tag, uint32_t keep) {
-            constexpr bool MASKED = decltype(masked_tag)::value;
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-              const uint32_t sc = score2_dyn(r < 4 ? wa.x : wa.y, r < 4 ? wb.x : wb.y, r);
-              uint32_t e = __viaddmax_u16x2(E[r], nge2, T[r]);
-              const uint32_t x = __viaddmax_u16x2(d, sc, e);
-              const uint32_t f = r == 0 ? fv : __viaddmax_u16x2(fv, nge2, xo);
-              uint32_t h = LOCAL ? __vimax3_u16x2(x, f, kBias2) : __vimax3_u16x2(x, f, f);
-              uint32_t tn = sub2_imad(h, one, neg_oe2);
-              xo = LOCAL ? __viaddmax_u16x2(x, noe2, zero_oe2) : sub2_imad(x, one, neg_oe2);
-              if constexpr (MASKED) {
-                h = (h & ~keep) | (H[r] & keep);
-                tn = (tn & ~keep) | (T[r] & keep);
-                e = (e & ~keep) | (E[r] & keep);
-              }
-              if constexpr (CHECK) hmax = __vimax3_u16x2(hmax, h, h);
-              if constexpr (LOCAL) {
-                // Halves where this cell beats the row's best so far
-                // (strictly, so the first column of a maximum is kept).
-                const uint32_t cm = __vcmpgtu2(h, best[r]);
-                best[r] = __vimax3_u16x2(best[r], h, h);
-                bcol[r] = (bcol[r] & ~cm) | (pack2(jA + 1, jB + 1) & cm);
-              }
-              d = H[r];
-              H[r] = h;
-              T[r] = tn;
-              E[r] = e;
-              fv = f;
-            }
-          };
-          if (vA && vB) {
-            hdiag = upH;
-            sweep(BoolTag<false>{}, 0u);
-          } else {
-            // Halves outside their column range keep their old values; a
-            // half that has not started keeps its left-boundary diagonal.
-            const uint32_t keep = vA ? 0xFFFF0000u : 0x0000FFFFu;
-            hdiag = (upH & ~keep) | (hdiag & keep);
-            sweep(BoolTag<true>{}, keep);
-          }
-          outH = H[R - 1];
-          outF = fv;
-          if (t == G - 1 && vB) top[jB] = prmt(outH, outF, 0x7632u);
-        }
+    for (int o = 16; o > 0; o >>= 1) n_min = min(n_min, __shfl_xor_sync(0xffffffffu, n_min, o));
+    const int i0 = min(2 * G, steps_pad);
+    const int i1 = max(i0, n_min & ~1);
+
+    auto step = [&](const int s, auto k_tag, auto interior_tag) {
+      constexpr int k = decltype(k_tag)::value;
+      constexpr bool INTERIOR = decltype(interior_tag)::value;
+      // Chunk boundaries fall on odd steps only (pairs start on even steps).
+      if (k == 1 && ((s + 1) & (kChunk - 1)) == 0) {
+        cp_async_wait_all();
+        __syncwarp();
+        stage_chunk_rt<uint32_t, kCodeRing16>(G, (s + 1) / kChunk + 1, t, nact, top, top_ring, A.codes, boff,
+                                              code_ring);
+        cp_async_commit();
       }
+      const uint32_t rH = __shfl_sync(0xffffffffu, outH, src_lane);
+      const uint32_t rF = __shfl_sync(0xffffffffu, outF, src_lane);
+      const int jA = s - t, jB = jA - G;
+      const uint2 wa = pa[k], wb = pb[k];
+      {
+        const int ca = min(int(code_ring[(boff + jA + 1) & (kCodeRing16 - 1)]), kLetters - 1);
+        const int cb = min(int(code_ring[(boff + jB + 1) & (kCodeRing16 - 1)]), kLetters - 1);
+        pa[k ^ 1] = profA[(2 * ca) * kThreads16];
+        pb[k ^ 1] = profB[(2 * cb) * kThreads16];
+      }
+      // Lane 0: band A from the staged top row, band B from lane G-1's
+      // band-A bottom; other lanes take the shuffled values whole.  Lane-
+      // dependent PRMT selectors instead of a branch; every lane of a group
+      // reads lane 0's ring entry (one broadcast address per group).
+      const uint32_t upH = prmt(tv[k], rH, selH);
+      const uint32_t upF = prmt(tv[k], rF, selF);
+      tv[k ^ 1] = top_ring[(s + 1) & (kTopRing - 1)];
+      const bool vA = INTERIOR || (unsigned)jA < (unsigned)nact;
+      const bool vB = INTERIOR || (unsigned)jB < (unsigned)nact;
+      if (vA || vB) {
+        uint32_t d = hdiag;
+        // F of the lane's first row from the row above it.
+        uint32_t fv = __viaddmax_u16x2(upF, nge2, __viaddmax_u16x2(upH, noe2, kNeg2));
+        uint32_t xo = 0u;
+        // Rows in order.  Since open >= 0, F(i+1,j) = max(F(i,j) - ext,
+        // max(X(i,j) [, 0]) - open - ext) with X = max(D + s, E): the only
+        // dependence between rows is one add-max on F.
+        auto sweep = [&](auto masked_tag, uint32_t keep) {
+          constexpr bool MASKED = decltype(masked_tag)::value;
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const uint32_t sc = score2_dyn(r < 4 ? wa.x : wa.y, r < 4 ? wb.x : wb.y, r);
+            uint32_t e = __viaddmax_u16x2(E[r], nge2, T[r]);
+            const uint32_t x = __viaddmax_u16x2(d, sc, e);
+            const uint32_t f = r == 0 ? fv : __viaddmax_u16x2(fv, nge2, xo);
+            uint32_t h = LOCAL ? __vimax3_u16x2(x, f, kBias2) : __vimax3_u16x2(x, f, f);
+            uint32_t tn = sub2_imad(h, one, neg_oe2);
+            xo = LOCAL ? __viaddmax_u16x2(x, noe2, zero_oe2) : sub2_imad(x, one, neg_oe2);
+            if constexpr (MASKED) {
+              h = (h & ~keep) | (H[r] & keep);
+              tn = (tn & ~keep) | (T[r] & keep);
+              e = (e & ~keep) | (E[r] & keep);
+            }
+            if constexpr (CHECK) hmax = __vimax3_u16x2(hmax, h, h);
+            if constexpr (LOCAL) {
+              // Halves where this cell beats the row's best so far
+              // (strictly, so the first column of a maximum is kept).
+              const uint32_t cm = __vcmpgtu2(h, best[r]);
+              best[r] = __vimax3_u16x2(best[r], h, h);
+              bcol[r] = (bcol[r] & ~cm) | (pack2(jA + 1, jB + 1) & cm);
+            }
+            d = H[r];
+            H[r] = h;
+            T[r] = tn;
+            E[r] = e;
+            fv = f;
+          }
+        };
+        if (INTERIOR || (vA && vB)) {
+          hdiag = upH;
+          sweep(BoolTag<false>{}, 0u);
+        } else {
+          // Halves outside their column range keep their old values; a
+          // half that has not started keeps its left-boundary diagonal.
+          const uint32_t keep = vA ? 0xFFFF0000u : 0x0000FFFFu;
+          hdiag = (upH & ~keep) | (hdiag & keep);
+          sweep(BoolTag<true>{}, keep);
+        }
+        outH = H[R - 1];
+        outF = fv;
+        if (t == G - 1 && vB) top[jB] = prmt(outH, outF, 0x7632u);
+      }
+    };
+    int s0 = 0;
+    for (; s0 < i0; s0 += 2) {
+      step(s0, IntTag<0>{}, BoolTag<false>{});
+      step(s0 + 1, IntTag<1>{}, BoolTag<false>{});
+    }
+    for (; s0 < i1; s0 += 2) {
+      step(s0, IntTag<0>{}, BoolTag<true>{});
+      step(s0 + 1, IntTag<1>{}, BoolTag<true>{});
+    }
+    for (; s0 < steps_pad; s0 += 2) {
+      step(s0, IntTag<0>{}, BoolTag<false>{});
+      step(s0 + 1, IntTag<1>{}, BoolTag<false>{});
     }
     cp_async_wait_all();
     __syncwarp();
