@@ -14,6 +14,16 @@ constexpr int kThreads = 256;   // 8 warps per block
 constexpr int kMatBytes = 704;  // 26*26 int8 rounded up to a 64-byte multiple
 constexpr int kAhead = 4;       // step-loop unroll
 
+// Compile-time flags for the step bodies.
+template <bool B>
+struct BoolTag {
+  static constexpr bool value = B;
+};
+template <int K>
+struct IntTag {
+  static constexpr int value = K;
+};
+
 // Sign-extends byte K of w to 32 bits with one PRMT (selector bit 3 of each
 // nibble replicates the sign of the chosen byte).
 template <int K>

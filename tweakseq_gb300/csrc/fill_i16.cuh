@@ -94,14 +94,6 @@ __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
   return d;
 }
 
-template <bool B>
-struct BoolTag {
-  static constexpr bool value = B;
-};
-template <int K>
-struct IntTag {
-  static constexpr int value = K;
-};
 
 // The lane width G is a run-time value: one code path serves every width,
 // which keeps the kernel small enough for the instruction cache.

@@ -185,137 +185,163 @@ __device__ __forceinline__ void fill_warp_task(const FillArgs &A, const int8_t *
       pw[0] = prof[cb[0] * kThreads];
       tv[0] = top_ring[0];
 
-      for (int s0 = 0; s0 < max_steps; s0 += kAhead) {
+      // Steps run in groups of kAhead (the count padded up; padding steps
+      // have every column out of range).  Steps [G, n_min) -- n_min the
+      // shortest column count of the warp's groups this band, 0 when one of
+      // them is idle -- have every lane in range: no range test there.
+      const int steps_pad = (max_steps + kAhead - 1) / kAhead * kAhead;
+      int n_min = nact;
 #pragma unroll
-        for (int k = 0; k < kAhead; ++k) {
-          const int s = s0 + k;
-          if (s < max_steps) {
-            if (((s + 1) & (kChunk - 1)) == 0) {
-              // Last step of a chunk: the next chunk (issued 32 steps ago)
-              // must have landed before this step reads its first column.
-              cp_async_wait_all();
-              __syncwarp();
-              stage_chunk<G>((s + 1) / kChunk + 1, t, nact, top, top_ring, A.codes, boff, code_ring);
-              cp_async_commit();
-            }
-            int32_t upH = __shfl_up_sync(0xffffffffu, outH, 1, G);
-            int32_t upF = __shfl_up_sync(0xffffffffu, outF, 1, G);
-            uint32_t upCH = 0, upCF = 0;
-            if constexpr (OUT == kOutIdent) {
-              upCH = __shfl_up_sync(0xffffffffu, outCH, 1, G);
-              upCF = __shfl_up_sync(0xffffffffu, outCF, 1, G);
-            }
-            const int jj = s - t;
-            const bool valid = (unsigned)jj < (unsigned)nact;
-            const int bc = cb[k & 1];
-            const uint2 pcur = pw[k & 1];
-            // Operands of the next step.  Codes outside the pair are clamped
-            // into the table; those steps are masked anyway.
-            cb[(k + 1) & 1] = min(int(code_ring[(boff + jj + 1) & (kCodeRing - 1)]), kLetters - 1);
-            pw[(k + 1) & 1] = prof[cb[(k + 1) & 1] * kThreads];
-            if (t == 0) {
-              upH = tv[k & 1].x;
-              upF = tv[k & 1].y;
-              if constexpr (OUT == kOutIdent) {
-                upCH = uint32_t(tv[k & 1].z);
-                upCF = uint32_t(tv[k & 1].w);
-              }
-              tv[(k + 1) & 1] = top_ring[(jj + 1) & (kTopRing - 1)];
-            }
-            if (valid) {
-              int32_t hu = upH, fv = upF, d = hdiag;
-              uint32_t chu = upCH, cfv = upCF, cd = cdiag;
-              hdiag = upH;
-              cdiag = upCH;
-              uint32_t tw = 0;
-#pragma unroll
-              for (int r = 0; r < R; ++r) {
-                const int32_t sc = sbyte_dyn(r < 4 ? pcur.x : pcur.y, r);
-                const int32_t eo = H[r] - oe, ee = E[r] - ge;
-                const int32_t fo = hu - oe, fe = fv - ge;
-                const int32_t e = max(eo, ee);
-                const int32_t f = max(fo, fe);
-                const int32_t dd = d + sc;
-                int32_t h;
-                if constexpr (OUT == kOutScore) {
-                  h = LOCAL ? __vimax3_s32_relu(dd, e, f) : __vimax3_s32(dd, e, f);
-                  if constexpr (LOCAL) {
-                    if (h > best[r]) {
-                      best[r] = h;
-                      bcol[r] = jj + 1;
-                    }
-                  }
-                } else {
-                  const bool eopen = eo >= ee, fopen = fo >= fe;
-                  int dir = kDirDiag;
-                  h = dd;
-                  if (e > h) {
-                    h = e;
-                    dir = kDirE;
-                  }
-                  if (f > h) {
-                    h = f;
-                    dir = kDirF;
-                  }
-                  if (LOCAL && h <= 0) {
-                    h = 0;
-                    dir = kDirStop;
-                  }
-                  if constexpr (OUT == kOutIdent) {
-                    const uint32_t ce = (eopen ? cH[r] : cE[r]) + kCol;
-                    const uint32_t cfn = (fopen ? chu : cfv) + kCol;
-                    const uint32_t cdd = cd + (qa[r] == bc ? kIdentCol : kCol);
-                    uint32_t ch = dir == kDirDiag ? cdd : (dir == kDirE ? ce : cfn);
-                    if (LOCAL && dir == kDirStop) ch = 0u;
-                    cd = cH[r];
-                    cH[r] = ch;
-                    cE[r] = ce;
-                    chu = ch;
-                    cfv = cfn;
-                    if constexpr (LOCAL) {
-                      if (h > best[r]) {
-                        best[r] = h;
-                        bcol[r] = jj + 1;
-                        bcnt[r] = ch;
-                      }
-                    }
-                  } else {
-                    tw |= uint32_t(dir | (eopen ? 4 : 0) | (fopen ? 8 : 0)) << (4 * r);
-                    if constexpr (LOCAL) {
-                      if (h > best[r]) {
-                        best[r] = h;
-                        bcol[r] = jj + 1;
-                      }
-                    }
-                  }
-                }
-                d = H[r];
-                H[r] = h;
-                E[r] = e;
-                hu = h;
-                fv = f;
-              }
-              outH = hu;
-              outF = fv;
-              outCH = chu;
-              outCF = cfv;
-              if (t == G - 1) {
-                Top v;
-                v.x = outH;
-                v.y = outF;
-                if constexpr (OUT == kOutIdent) {
-                  v.z = int32_t(outCH);
-                  v.w = int32_t(outCF);
-                }
-                top[jj] = v;
-              }
-              if constexpr (OUT == kOutTrace) {
-                const int64_t entry = ((int64_t)pass * (n + G - 1) + s) * G + t;
-                reinterpret_cast<uint32_t *>(planes)[entry] = tw;
-              }
-            }
+      for (int o = 16; o > 0; o >>= 1) n_min = min(n_min, __shfl_xor_sync(0xffffffffu, n_min, o));
+      const int i0 = min(G, steps_pad);
+      const int i1 = max(i0, n_min / kAhead * kAhead);
+      auto step = [&](const int s, auto k_tag, auto interior_tag) {
+        constexpr int k = decltype(k_tag)::value;
+        constexpr bool INTERIOR = decltype(interior_tag)::value;
+        if (k == kAhead - 1 && ((s + 1) & (kChunk - 1)) == 0) {
+          // Last step of a chunk: the next chunk (issued 32 steps ago) must
+          // have landed before this step reads its first column.
+          cp_async_wait_all();
+          __syncwarp();
+          stage_chunk<G>((s + 1) / kChunk + 1, t, nact, top, top_ring, A.codes, boff, code_ring);
+          cp_async_commit();
+        }
+        int32_t upH = __shfl_up_sync(0xffffffffu, outH, 1, G);
+        int32_t upF = __shfl_up_sync(0xffffffffu, outF, 1, G);
+        uint32_t upCH = 0, upCF = 0;
+        if constexpr (OUT == kOutIdent) {
+          upCH = __shfl_up_sync(0xffffffffu, outCH, 1, G);
+          upCF = __shfl_up_sync(0xffffffffu, outCF, 1, G);
+        }
+        const int jj = s - t;
+        const bool valid = INTERIOR || (unsigned)jj < (unsigned)nact;
+        const int bc = cb[k & 1];
+        const uint2 pcur = pw[k & 1];
+        // Operands of the next step.  Codes outside the pair are clamped
+        // into the table; those steps are masked anyway.
+        cb[(k + 1) & 1] = min(int(code_ring[(boff + jj + 1) & (kCodeRing - 1)]), kLetters - 1);
+        pw[(k + 1) & 1] = prof[cb[(k + 1) & 1] * kThreads];
+        // Lane 0 takes the staged top row (selects, not a branch); every
+        // lane of a group reads lane 0's ring entry (one address per group).
+        if (t == 0) {
+          upH = tv[k & 1].x;
+          upF = tv[k & 1].y;
+          if constexpr (OUT == kOutIdent) {
+            upCH = uint32_t(tv[k & 1].z);
+            upCF = uint32_t(tv[k & 1].w);
           }
         }
+        tv[(k + 1) & 1] = top_ring[(s + 1) & (kTopRing - 1)];
+        if (valid) {
+          int32_t hu = upH, fv = upF, d = hdiag;
+          uint32_t chu = upCH, cfv = upCF, cd = cdiag;
+          hdiag = upH;
+          cdiag = upCH;
+          uint32_t tw = 0;
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const int32_t sc = sbyte_dyn(r < 4 ? pcur.x : pcur.y, r);
+            const int32_t eo = H[r] - oe, ee = E[r] - ge;
+            const int32_t fo = hu - oe, fe = fv - ge;
+            const int32_t e = max(eo, ee);
+            const int32_t f = max(fo, fe);
+            const int32_t dd = d + sc;
+            int32_t h;
+            if constexpr (OUT == kOutScore) {
+              h = LOCAL ? __vimax3_s32_relu(dd, e, f) : __vimax3_s32(dd, e, f);
+              if constexpr (LOCAL) {
+                if (h > best[r]) {
+                  best[r] = h;
+                  bcol[r] = jj + 1;
+                }
+              }
+            } else {
+              const bool eopen = eo >= ee, fopen = fo >= fe;
+              int dir = kDirDiag;
+              h = dd;
+              if (e > h) {
+                h = e;
+                dir = kDirE;
+              }
+              if (f > h) {
+                h = f;
+                dir = kDirF;
+              }
+              if (LOCAL && h <= 0) {
+                h = 0;
+                dir = kDirStop;
+              }
+              if constexpr (OUT == kOutIdent) {
+                const uint32_t ce = (eopen ? cH[r] : cE[r]) + kCol;
+                const uint32_t cfn = (fopen ? chu : cfv) + kCol;
+                const uint32_t cdd = cd + (qa[r] == bc ? kIdentCol : kCol);
+                uint32_t ch = dir == kDirDiag ? cdd : (dir == kDirE ? ce : cfn);
+                if (LOCAL && dir == kDirStop) ch = 0u;
+                cd = cH[r];
+                cH[r] = ch;
+                cE[r] = ce;
+                chu = ch;
+                cfv = cfn;
+                if constexpr (LOCAL) {
+                  if (h > best[r]) {
+                    best[r] = h;
+                    bcol[r] = jj + 1;
+                    bcnt[r] = ch;
+                  }
+                }
+              } else {
+                tw |= uint32_t(dir | (eopen ? 4 : 0) | (fopen ? 8 : 0)) << (4 * r);
+                if constexpr (LOCAL) {
+                  if (h > best[r]) {
+                    best[r] = h;
+                    bcol[r] = jj + 1;
+                  }
+                }
+              }
+            }
+            d = H[r];
+            H[r] = h;
+            E[r] = e;
+            hu = h;
+            fv = f;
+          }
+          outH = hu;
+          outF = fv;
+          outCH = chu;
+          outCF = cfv;
+          if (t == G - 1) {
+            Top v;
+            v.x = outH;
+            v.y = outF;
+            if constexpr (OUT == kOutIdent) {
+              v.z = int32_t(outCH);
+              v.w = int32_t(outCF);
+            }
+            top[jj] = v;
+          }
+          if constexpr (OUT == kOutTrace) {
+            const int64_t entry = ((int64_t)pass * (n + G - 1) + s) * G + t;
+            reinterpret_cast<uint32_t *>(planes)[entry] = tw;
+          }
+        }
+      };
+      auto run = [&](int from, int to, auto interior_tag) {
+        for (int s0 = from; s0 < to; s0 += kAhead) {
+          step(s0, IntTag<0>{}, interior_tag);
+          step(s0 + 1, IntTag<1>{}, interior_tag);
+          step(s0 + 2, IntTag<2>{}, interior_tag);
+          step(s0 + 3, IntTag<3>{}, interior_tag);
+        }
+      };
+      static_assert(kAhead == 4, "the step runs below are unrolled by 4");
+      // One copy of each body: the ramp-up and ramp-down segments share the
+      // general one.
+#pragma unroll 1
+      for (int seg = 0; seg < 3; ++seg) {
+        if (seg == 1)
+          run(i0, i1, BoolTag<true>{});
+        else
+          run(seg == 0 ? 0 : i1, seg == 0 ? i0 : steps_pad, BoolTag<false>{});
       }
       cp_async_wait_all();
       __syncwarp();
