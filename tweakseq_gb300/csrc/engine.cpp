@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
+#include <thread>
 
 namespace tsq {
 
@@ -71,14 +72,60 @@ int cuda_status(cudaError_t e) {
 namespace {
 
 int pow2ceil(int64_t x) {
-  int v = 1;
-  while (v < x && v < (1 << 30)) v <<= 1;
-  return v;
+  if (x <= 1) return 1;
+  if (x >= (int64_t(1) << 30)) return 1 << 30;
+  return 1 << (64 - __builtin_clzll(uint64_t(x - 1)));
 }
 
 constexpr int kR = 8;
 // Longest sequence the int32 kernels take: coordinates travel in 20 bits.
 constexpr int64_t kMaxLen = (1 << 20) - 1;
+
+// Runs f(begin, end, slot) over [0, n) on up to 8 host threads (slot =
+// 0..threads-1), one thread when n is small.  Returns the thread count.
+template <class F>
+int parallel_for(int64_t n, F &&f) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int threads = int(std::min<int64_t>({8, int64_t(hw), std::max<int64_t>(1, n / 16384)}));
+  if (threads <= 1) {
+    f(int64_t(0), n, 0);
+    return 1;
+  }
+  const int64_t chunk = (n + threads - 1) / threads;
+  std::vector<std::thread> th;
+  th.reserve(size_t(threads - 1));
+  for (int i = 1; i < threads; ++i)
+    th.emplace_back([&f, i, chunk, n] { f(std::min(n, i * chunk), std::min(n, (i + 1) * chunk), i); });
+  f(int64_t(0), std::min(n, chunk), 0);
+  for (std::thread &x : th) x.join();
+  return threads;
+}
+
+// Stable LSD radix sort by key (ascending) in 11-bit digits over the low
+// `bits` bits; a digit that is the same for every record costs only its
+// count.  tmp is scratch of the same size.
+void radix_sort(std::vector<SortRec> &a, std::vector<SortRec> &tmp, int bits) {
+  if (tmp.size() < a.size()) tmp.resize(a.size());
+  std::vector<uint32_t> cnt(1u << 11);
+  for (int shift = 0; shift < bits; shift += 11) {
+    std::fill(cnt.begin(), cnt.end(), 0u);
+    for (const SortRec &r : a) ++cnt[(r.key >> shift) & 2047u];
+    if (std::find(cnt.begin(), cnt.end(), uint32_t(a.size())) != cnt.end()) continue;
+    uint32_t sum = 0;
+    for (uint32_t &c : cnt) {
+      const uint32_t v = c;
+      c = sum;
+      sum += v;
+    }
+    for (const SortRec &r : a) tmp[cnt[(r.key >> shift) & 2047u]++] = r;
+    const size_t na = a.size(), nt = tmp.size();
+    a.swap(tmp);
+    a.resize(na);
+    tmp.resize(std::max(nt, na));
+  }
+}
+
+int bit_width(uint64_t v) { return v == 0 ? 0 : 64 - __builtin_clzll(v); }
 
 }  // namespace
 
@@ -182,24 +229,59 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
 
   // Validate the pair table and the value range the int32 kernels assume:
   // every H, E, F stays above -(3*open + (m+n+1)*ext + 128), which must be
-  // far from the kernels' "minus infinity" (-2^29).
+  // far from the kernels' "minus infinity" (-2^29).  Parallel over the
+  // pairs; the error reported is that of the first bad pair.
   b->pairs_h.resize(size_t(n));
+  struct ValPart {
+    int64_t cells = 0, bad_at = INT64_MAX;
+    int32_t max_n = 0;
+    int rc = TSQ_OK;
+  };
+  std::vector<ValPart> vparts(8);
+  parallel_for(n, [&](int64_t lo, int64_t hi, int slot) {
+    ValPart v;
+    for (int64_t k = lo; k < hi; ++k) {
+      const tsq_pair_desc &d = pairs[k];
+      int rc = TSQ_OK;
+      if (d.a_len < 0 || d.b_len < 0 || d.a_off < 0 || d.b_off < 0)
+        rc = TSQ_E_INVALID_ARG;
+      else if (d.a_off > seqs_len - d.a_len || d.b_off > seqs_len - d.b_len)
+        rc = TSQ_E_INVALID_ARG;
+      else if (d.a_len > kMaxLen || d.b_len > kMaxLen)
+        rc = TSQ_E_TOO_LARGE;
+      else if (3 * int64_t(p->gap_open) + (int64_t(d.a_len) + d.b_len + 1) * p->gap_extend + 128 >=
+               (int64_t(1) << 28))
+        rc = TSQ_E_TOO_LARGE;
+      else if (b->out_mode == kOutIdent && int64_t(d.a_len) + d.b_len > 65535)
+        rc = TSQ_E_TOO_LARGE;
+      // Local maxima travel in 24 bits of the reduction key.
+      else if (p->mode == TSQ_LOCAL && int64_t(std::max(sc.max_score, 0)) * std::min(d.a_len, d.b_len) >= (1 << 23))
+        rc = TSQ_E_TOO_LARGE;
+      if (rc != TSQ_OK) {
+        v.bad_at = k;
+        v.rc = rc;
+        break;
+      }
+      b->pairs_h[size_t(k)] = PairDev{d.a_off, d.b_off, d.a_len, d.b_len};
+      v.cells += int64_t(d.a_len) * d.b_len;
+      v.max_n = std::max(v.max_n, d.b_len);
+    }
+    vparts[size_t(slot)] = v;
+  });
   int64_t cells = 0;
   int32_t max_n = 0;
-  for (int64_t k = 0; k < n; ++k) {
-    const tsq_pair_desc &d = pairs[k];
-    if (d.a_len < 0 || d.b_len < 0 || d.a_off < 0 || d.b_off < 0) return TSQ_E_INVALID_ARG;
-    if (d.a_off > seqs_len - d.a_len || d.b_off > seqs_len - d.b_len) return TSQ_E_INVALID_ARG;
-    if (d.a_len > kMaxLen || d.b_len > kMaxLen) return TSQ_E_TOO_LARGE;
-    const int64_t low = 3 * int64_t(p->gap_open) + (int64_t(d.a_len) + d.b_len + 1) * p->gap_extend + 128;
-    if (low >= (int64_t(1) << 28)) return TSQ_E_TOO_LARGE;
-    if (b->out_mode == kOutIdent && int64_t(d.a_len) + d.b_len > 65535) return TSQ_E_TOO_LARGE;
-    // Local maxima travel in 24 bits of the reduction key.
-    if (p->mode == TSQ_LOCAL && int64_t(std::max(sc.max_score, 0)) * std::min(d.a_len, d.b_len) >= (1 << 23))
-      return TSQ_E_TOO_LARGE;
-    b->pairs_h[size_t(k)] = PairDev{d.a_off, d.b_off, d.a_len, d.b_len};
-    cells += int64_t(d.a_len) * d.b_len;
-    max_n = std::max(max_n, d.b_len);
+  {
+    int64_t bad_at = INT64_MAX;
+    int bad_rc = TSQ_OK;
+    for (const ValPart &v : vparts) {
+      cells += v.cells;
+      max_n = std::max(max_n, v.max_n);
+      if (v.bad_at < bad_at) {
+        bad_at = v.bad_at;
+        bad_rc = v.rc;
+      }
+    }
+    if (bad_rc != TSQ_OK) return bad_rc;
   }
   b->cells = cells;
 
@@ -213,49 +295,26 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   } sync_on_exit{b->stream};
   if (seqs_len > 0) TSQ_TRY(cudaMemcpyAsync(b->seqs.p, seqs, size_t(seqs_len), cudaMemcpyHostToDevice, b->stream));
 
-  // ---- lane types ------------------------------------------------------
+  // ---- lane types, shapes and order (one parallel pass over the pairs) ----
   // Score fills run in int16x2 when the pair's values provably fit: the
   // upper bound max_score * min(m, n) (unchecked kernel) and the lower
   // bound -(3*open + (m + 512 + n + 1)*ext + open + ext + 128 + |min|),
   // 512 being the most padding rows a pass can add, against the int16
-  // kernels' minus infinity (-32000).  Pairs with the lower bound but not
-  // the upper one run the overflow-checked int16x2 kernel and are re-run
-  // in int32 if flagged; everything else runs in int32.
-  std::vector<int8_t> lsel(static_cast<size_t>(n));
-  int64_t n_checked = 0;
-  for (int64_t k = 0; k < n; ++k) {
-    const PairDev &pd = b->pairs_h[size_t(k)];
-    int8_t lt = 0;
-    if (b->out_mode == kOutScore && p->lane != TSQ_LANE_I32) {
-      const int64_t go = p->gap_open, ge = p->gap_extend;
-      const int64_t lowest = 3 * go + (int64_t(pd.a_len) + 512 + pd.b_len + 1) * ge + go + ge + 128 +
-                             std::max<int64_t>(0, -int64_t(sc.min_score));
-      // The int16x2 kernel also subtracts open + ext from values at this
-      // bound (T and XO), which must stay above -32768.
-      const bool lower_ok = lowest + go + ge < 31000 && ge <= 700 && pd.b_len <= 65535;
-      const bool upper_ok =
-          int64_t(std::max(sc.max_score, 0)) * std::min(pd.a_len, pd.b_len) + std::max(sc.max_score, 0) < 32767;
-      if (lower_ok) lt = (upper_ok && p->lane == TSQ_LANE_AUTO) ? 1 : 2;
-    }
-    lsel[size_t(k)] = lt;
-    n_checked += lt == 2;
-  }
+  // kernels' minus infinity (-32000); the int16x2 kernel also subtracts
+  // open + ext from values at this bound (T and XO), which must stay above
+  // -32768.  Pairs with the lower bound but not the upper one run the
+  // overflow-checked int16x2 kernel and are re-run in int32 if flagged;
+  // everything else runs in int32.
+  //
   // Long int32 pairs go to the CTA fill (their bands striped over 8 warps):
   // those whose sweep on one 32-lane group -- ceil(m/256) bands of n+31
   // steps -- would outlast the batch's balanced per-lane work (or, alone,
   // 20,000 steps).
-  {
-    const double lanes = double(sms) * 24.0 * 32.0;
-    const double budget = std::max(20000.0, plain ? 0.0 : double(cells) / (lanes * kR));
-    for (int64_t k = 0; k < n; ++k) {
-      if (lsel[size_t(k)] != 0) continue;
-      const PairDev &pd = b->pairs_h[size_t(k)];
-      const double steps32 = double((pd.a_len + 255) / 256) * double(pd.b_len + 31);
-      if (pd.a_len > 0 && pd.b_len > 0 && steps32 > budget) lsel[size_t(k)] = 3;
-    }
-  }
-
-  // ---- shapes and buckets ----------------------------------------------
+  //
+  // Order: lane type (CTA, checked int16x2, int16x2, int32), then lane
+  // width, then bands and columns descending, then input order -- one
+  // 44-bit key, sorted by a stable LSD radix sort (O(n): the plan of an
+  // 8M-pair batch must not cost seconds).
   ShapeChooser ch;
   ch.out_mode = b->out_mode;
   ch.local = b->local;
@@ -266,60 +325,99 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
     ch.avg_lane_steps = double(cells) / (lanes * kR);
   }
   ch.use_table = b->autotune && tune_table_loaded();
-  std::vector<int32_t> gsel(static_cast<size_t>(n));
-  std::vector<int32_t> rsel(static_cast<size_t>(n));
-  std::vector<int32_t> order(static_cast<size_t>(n));
-  for (int64_t k = 0; k < n; ++k) {
-    const int rows_per_lane = (lsel[size_t(k)] == 1 || lsel[size_t(k)] == 2) ? 2 * kR : kR;
-    Shape s = ch.pick(b->pairs_h[size_t(k)].a_len, b->pairs_h[size_t(k)].b_len, rows_per_lane);
-    if (lsel[size_t(k)] == 3) s = Shape{32, kR, 0};  // one 32-lane group per warp of the CTA
-    s.i16 = 0;
-    if (!shape_supported(s, b->out_mode, b->local)) return TSQ_E_INVALID_ARG;
-    gsel[size_t(k)] = s.G;
-    rsel[size_t(k)] = s.R;
-    order[size_t(k)] = int32_t(k);
-  }
-  // Bands and steps of a pair's sweep under its lane type and shape.
-  auto two_bands = [&](int32_t k) { return lsel[size_t(k)] == 1 || lsel[size_t(k)] == 2; };
-  auto bands = [&](int32_t k) {
+  PlanScratch &ps = b->scratch;
+  ps.lsel.resize(size_t(n));
+  ps.gsel.resize(size_t(n));
+  ps.rsel.resize(size_t(n));
+  ps.recs.resize(size_t(n));
+  std::vector<int8_t> &lsel = ps.lsel;
+  std::vector<int32_t> &gsel = ps.gsel;
+  std::vector<int32_t> &rsel = ps.rsel;
+  std::vector<SortRec> &recs = ps.recs;
+  auto two_bands = [&](int64_t k) { return lsel[size_t(k)] == 1 || lsel[size_t(k)] == 2; };
+  auto bands = [&](int64_t k) {
     const int P = gsel[size_t(k)] * rsel[size_t(k)] * (two_bands(k) ? 2 : 1);
     return (b->pairs_h[size_t(k)].a_len + P - 1) / P;
   };
-  auto steps = [&](int32_t k) {
+  auto steps = [&](int64_t k) {
     return b->pairs_h[size_t(k)].b_len + gsel[size_t(k)] * (two_bands(k) ? 2 : 1) - 1;
   };
-  // Order: lane type (checked int16x2, int16x2, int32), then lane width,
-  // then bands and columns descending, then input order -- as one 44-bit
-  // key sorted by a stable LSD radix sort (O(n), the plan of an 8M-pair
-  // batch must not cost seconds).
+  struct ShapePart {
+    int64_t n_checked = 0;
+    uint64_t buckets[3] = {0, 0, 0};  // bit (G*4 + lane type) seen
+    bool bad_shape = false;
+    int32_t max_bands = 0, max_cols = 0;
+  };
+  std::vector<ShapePart> sparts(8);
   {
-    std::vector<uint64_t> key(static_cast<size_t>(n));
-    for (int64_t k = 0; k < n; ++k) {
-      const int gi = gsel[size_t(k)] == 4 ? 0 : gsel[size_t(k)] == 8 ? 1 : gsel[size_t(k)] == 16 ? 2 : 3;
-      const uint64_t bandk = uint64_t(std::min(bands(int32_t(k)), (1 << 19) - 1));
-      const uint64_t colk = uint64_t(std::min(b->pairs_h[size_t(k)].b_len, (1 << 20) - 1));
-      static const uint64_t kLaneRank[4] = {3, 2, 1, 0};  // CTA, checked int16x2, int16x2, int32
-      key[size_t(k)] = (kLaneRank[lsel[size_t(k)]] << 42) | (uint64_t(gi) << 40) |
-                       (((1ull << 19) - 1 - bandk) << 20) | ((1ull << 20) - 1 - colk);
-    }
-    std::vector<int32_t> tmp(static_cast<size_t>(n));
-    std::vector<uint32_t> cnt(1u << 11);
-    for (int shift = 0; shift < 44; shift += 11) {  // 2 bits of lane rank above the 42 key bits
-      std::fill(cnt.begin(), cnt.end(), 0u);
-      for (int64_t q = 0; q < n; ++q) ++cnt[(key[size_t(order[size_t(q)])] >> shift) & 2047u];
-      uint32_t sum = 0;
-      for (uint32_t &c : cnt) {
-        const uint32_t v = c;
-        c = sum;
-        sum += v;
+    const double lanes = double(sms) * 24.0 * 32.0;
+    const double cta_budget = std::max(20000.0, plain ? 0.0 : double(cells) / (lanes * kR));
+    const int64_t go = p->gap_open, ge = p->gap_extend;
+    const bool try16 = b->out_mode == kOutScore && p->lane != TSQ_LANE_I32;
+    const int64_t smax = std::max(sc.max_score, 0), sneg = std::max<int64_t>(0, -int64_t(sc.min_score));
+    parallel_for(n, [&](int64_t lo, int64_t hi, int slot) {
+      ShapePart sp;
+      for (int64_t k = lo; k < hi; ++k) {
+        const PairDev &pd = b->pairs_h[size_t(k)];
+        int8_t lt = 0;
+        if (try16) {
+          const int64_t lowest = 3 * go + (int64_t(pd.a_len) + 512 + pd.b_len + 1) * ge + go + ge + 128 + sneg;
+          const bool lower_ok = lowest + go + ge < 31000 && ge <= 700 && pd.b_len <= 65535;
+          const bool upper_ok = smax * std::min(pd.a_len, pd.b_len) + smax < 32767;
+          if (lower_ok) lt = (upper_ok && p->lane == TSQ_LANE_AUTO) ? 1 : 2;
+        }
+        if (lt == 0) {
+          const double steps32 = double((pd.a_len + 255) / 256) * double(pd.b_len + 31);
+          if (pd.a_len > 0 && pd.b_len > 0 && steps32 > cta_budget) lt = 3;
+        }
+        lsel[size_t(k)] = lt;
+        sp.n_checked += lt == 2;
+        const int rows_per_lane = (lt == 1 || lt == 2) ? 2 * kR : kR;
+        Shape shp = ch.pick(pd.a_len, pd.b_len, rows_per_lane);
+        if (lt == 3) shp = Shape{32, kR, 0};  // one 32-lane group per warp of the CTA
+        shp.i16 = 0;
+        if (!shape_supported(shp, b->out_mode, b->local)) sp.bad_shape = true;
+        gsel[size_t(k)] = shp.G;
+        rsel[size_t(k)] = shp.R;
+        const int bit = shp.G * 4 + lt;
+        sp.buckets[bit >> 6] |= uint64_t(1) << (bit & 63);
+        const int gi = shp.G == 4 ? 0 : shp.G == 8 ? 1 : shp.G == 16 ? 2 : 3;
+        const int32_t bandk = std::min(bands(k), (1 << 19) - 1);
+        const int32_t colk = std::min(pd.b_len, (1 << 20) - 1);
+        sp.max_bands = std::max(sp.max_bands, bandk);
+        sp.max_cols = std::max(sp.max_cols, colk);
+        static const uint64_t kLaneRank[4] = {3, 2, 1, 0};  // CTA, checked int16x2, int16x2, int32
+        // Provisional key; packed to the bits the batch needs below.
+        recs[size_t(k)] = SortRec{(kLaneRank[lt] << 42) | (uint64_t(gi) << 40) | (uint64_t(bandk) << 20) |
+                                      uint64_t(colk),
+                                  int32_t(k)};
       }
-      for (int64_t q = 0; q < n; ++q) {
-        const int32_t k = order[size_t(q)];
-        tmp[cnt[(key[size_t(k)] >> shift) & 2047u]++] = k;
-      }
-      order.swap(tmp);
-    }
+      sparts[size_t(slot)] = sp;
+    });
   }
+  int64_t n_checked = 0;
+  uint64_t bucket_bits[3] = {0, 0, 0};
+  int32_t max_bands = 0, max_cols = 0;
+  for (const ShapePart &sp : sparts) {
+    if (sp.bad_shape) return TSQ_E_INVALID_ARG;
+    n_checked += sp.n_checked;
+    for (int w = 0; w < 3; ++w) bucket_bits[w] |= sp.buckets[w];
+    max_bands = std::max(max_bands, sp.max_bands);
+    max_cols = std::max(max_cols, sp.max_cols);
+  }
+  {
+    // Pack (lane rank, lane width, bands descending, columns descending)
+    // into as few bits as this batch needs: fewer radix passes.
+    const int wb = bit_width(uint64_t(max_bands)), wc = bit_width(uint64_t(max_cols));
+    for (SortRec &r : recs) {
+      const uint64_t top = r.key >> 40, bandk = (r.key >> 20) & ((1u << 20) - 1), colk = r.key & ((1u << 20) - 1);
+      r.key = (top << (wb + wc)) | ((uint64_t(max_bands) - bandk) << wc) | (uint64_t(max_cols) - colk);
+    }
+    radix_sort(recs, ps.tmp, 4 + wb + wc);
+  }
+  ps.order.resize(size_t(n));
+  std::vector<int32_t> &order = ps.order;
+  for (int64_t q = 0; q < n; ++q) order[size_t(q)] = recs[size_t(q)].idx;
 
   // One launch per lane type (int16x2 checked, int16x2, int32), each a list
   // of warp tasks -- consecutive pairs of one lane width, 32/G per warp --
@@ -358,6 +456,8 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
     }
     std::vector<int2> wt;
     std::vector<int64_t> wcost;
+    wt.reserve(size_t(e - s));
+    wcost.reserve(size_t(e - s));
     for (int64_t q = s; q < e;) {
       const int G = gsel[size_t(order[size_t(q)])];
       const int per = 32 / G;
@@ -372,10 +472,14 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
       wcost.push_back(cost);
       q = r;
     }
+    // Longest first: ascending order of (max cost - cost), stable.
+    int64_t max_cost = 0;
+    for (int64_t c : wcost) max_cost = std::max(max_cost, c);
+    std::vector<SortRec> wrec(wt.size());
+    for (size_t w = 0; w < wt.size(); ++w) wrec[w] = SortRec{uint64_t(max_cost - wcost[w]), int32_t(w)};
+    radix_sort(wrec, ps.tmp, bit_width(uint64_t(max_cost)));
     std::vector<int32_t> worder(wt.size());
-    std::iota(worder.begin(), worder.end(), 0);
-    std::stable_sort(worder.begin(), worder.end(),
-                     [&](int32_t x, int32_t y) { return wcost[size_t(x)] > wcost[size_t(y)]; });
+    for (size_t w = 0; w < wt.size(); ++w) worder[w] = wrec[w].idx;
     Launch L;
     L.R = kR;
     L.i16 = lt;
@@ -421,12 +525,8 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   b->stats.pairs = n;
   b->stats.cells = cells;
   b->stats.launches = int32_t(b->launches.size()) + 1 + (b->out_mode == kOutTrace ? 1 : 0) + (n_checked > 0 ? 1 : 0);
-  {
-    std::vector<int32_t> gs;
-    for (int64_t k = 0; k < n; ++k) gs.push_back(gsel[size_t(k)] * 4 + lsel[size_t(k)]);
-    std::sort(gs.begin(), gs.end());
-    b->stats.buckets = int32_t(std::unique(gs.begin(), gs.end()) - gs.begin());
-  }
+  b->stats.buckets = __builtin_popcountll(bucket_bits[0]) + __builtin_popcountll(bucket_bits[1]) +
+                      __builtin_popcountll(bucket_bits[2]);
   const std::vector<int2> &wt_sorted = wt_all;
 
   // ---- traceback layout ----------------------------------------------------

@@ -68,6 +68,20 @@ struct ShapeChooser {
   Shape pick(int m, int n, int rows_per_lane) const;
 };
 
+// Record of the planner's radix sorts.
+struct SortRec {
+  uint64_t key;
+  int32_t idx;
+};
+
+// Host scratch of the planner, kept by the batch object so that repeated
+// plans of similar batches neither allocate nor clear it.
+struct PlanScratch {
+  std::vector<int8_t> lsel;
+  std::vector<int32_t> gsel, rsel, order;
+  std::vector<SortRec> recs, tmp;
+};
+
 bool tune_table_loaded();
 bool tune_forced();
 bool tune_table_pick(int out_mode, int m, int n, Shape *sh);
@@ -94,6 +108,7 @@ struct tsq_batch {
   int64_t seqs_len = 0;
   int64_t cells = 0;
   std::vector<tsq::PairDev> pairs_h;
+  tsq::PlanScratch scratch;
   std::vector<tsq::Launch> launches;
   std::vector<int64_t> aln_off_h;
   int64_t aln_bytes = 0;
