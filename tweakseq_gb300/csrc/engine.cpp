@@ -103,26 +103,26 @@ int parallel_for(int64_t n, F &&f) {
 
 // Stable LSD radix sort by key (ascending) in 11-bit digits over the low
 // `bits` bits; a digit that is the same for every record costs only its
-// count.  tmp is scratch of the same size.
+// count.  tmp is scratch (grown to the size of a when smaller).
 void radix_sort(std::vector<SortRec> &a, std::vector<SortRec> &tmp, int bits) {
-  if (tmp.size() < a.size()) tmp.resize(a.size());
-  std::vector<uint32_t> cnt(1u << 11);
+  const size_t n = a.size();
+  if (tmp.size() < n) tmp.resize(n);
+  SortRec *src = a.data(), *dst = tmp.data();
+  uint32_t cnt[1u << 11];
   for (int shift = 0; shift < bits; shift += 11) {
-    std::fill(cnt.begin(), cnt.end(), 0u);
-    for (const SortRec &r : a) ++cnt[(r.key >> shift) & 2047u];
-    if (std::find(cnt.begin(), cnt.end(), uint32_t(a.size())) != cnt.end()) continue;
+    std::fill(cnt, cnt + (1u << 11), 0u);
+    for (size_t q = 0; q < n; ++q) ++cnt[(src[q].key >> shift) & 2047u];
+    if (std::find(cnt, cnt + (1u << 11), uint32_t(n)) != cnt + (1u << 11)) continue;
     uint32_t sum = 0;
     for (uint32_t &c : cnt) {
       const uint32_t v = c;
       c = sum;
       sum += v;
     }
-    for (const SortRec &r : a) tmp[cnt[(r.key >> shift) & 2047u]++] = r;
-    const size_t na = a.size(), nt = tmp.size();
-    a.swap(tmp);
-    a.resize(na);
-    tmp.resize(std::max(nt, na));
+    for (size_t q = 0; q < n; ++q) dst[cnt[(src[q].key >> shift) & 2047u]++] = src[q];
+    std::swap(src, dst);
   }
+  if (src != a.data()) std::copy(src, src + n, a.data());
 }
 
 int bit_width(uint64_t v) { return v == 0 ? 0 : 64 - __builtin_clzll(v); }
@@ -330,6 +330,7 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   ps.gsel.resize(size_t(n));
   ps.rsel.resize(size_t(n));
   ps.recs.resize(size_t(n));
+  ps.cost.resize(size_t(n));
   std::vector<int8_t> &lsel = ps.lsel;
   std::vector<int32_t> &gsel = ps.gsel;
   std::vector<int32_t> &rsel = ps.rsel;
@@ -384,6 +385,7 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
         const int gi = shp.G == 4 ? 0 : shp.G == 8 ? 1 : shp.G == 16 ? 2 : 3;
         const int32_t bandk = std::min(bands(k), (1 << 19) - 1);
         const int32_t colk = std::min(pd.b_len, (1 << 20) - 1);
+        ps.cost[size_t(k)] = int64_t(bands(k)) * steps(k);
         sp.max_bands = std::max(sp.max_bands, bandk);
         sp.max_cols = std::max(sp.max_cols, colk);
         static const uint64_t kLaneRank[4] = {3, 2, 1, 0};  // CTA, checked int16x2, int16x2, int32
@@ -416,8 +418,21 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
     radix_sort(recs, ps.tmp, 4 + wb + wc);
   }
   ps.order.resize(size_t(n));
+  ps.s_lt.resize(size_t(n));
+  ps.s_g.resize(size_t(n));
+  ps.s_cols.resize(size_t(n));
+  ps.s_cost.resize(size_t(n));
   std::vector<int32_t> &order = ps.order;
-  for (int64_t q = 0; q < n; ++q) order[size_t(q)] = recs[size_t(q)].idx;
+  parallel_for(n, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t q = lo; q < hi; ++q) {
+      const int32_t k = recs[size_t(q)].idx;
+      order[size_t(q)] = k;
+      ps.s_lt[size_t(q)] = lsel[size_t(k)];
+      ps.s_g[size_t(q)] = gsel[size_t(k)];
+      ps.s_cols[size_t(q)] = b->pairs_h[size_t(k)].b_len;
+      ps.s_cost[size_t(q)] = ps.cost[size_t(k)];
+    }
+  });
 
   // One launch per lane type (int16x2 checked, int16x2, int32), each a list
   // of warp tasks -- consecutive pairs of one lane width, 32/G per warp --
@@ -427,11 +442,11 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   int64_t bnd_total = 0;
   int32_t checked_begin = 0;
   for (int64_t s = 0; s < n;) {
-    const int8_t lt = lsel[size_t(order[size_t(s)])];
+    const int8_t lt = ps.s_lt[size_t(s)];
     int64_t e = s;
     int32_t cols = 1;
-    while (e < n && lsel[size_t(order[size_t(e)])] == lt) {
-      cols = std::max(cols, b->pairs_h[size_t(order[size_t(e)])].b_len);
+    while (e < n && ps.s_lt[size_t(e)] == lt) {
+      cols = std::max(cols, ps.s_cols[size_t(e)]);
       ++e;
     }
     if (lt == 2) checked_begin = int32_t(s);
@@ -459,13 +474,12 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
     wt.reserve(size_t(e - s));
     wcost.reserve(size_t(e - s));
     for (int64_t q = s; q < e;) {
-      const int G = gsel[size_t(order[size_t(q)])];
+      const int G = ps.s_g[size_t(q)];
       const int per = 32 / G;
       int64_t r = q;
       int64_t cost = 0;
-      while (r < e && r - q < per && gsel[size_t(order[size_t(r)])] == G) {
-        const int32_t k = order[size_t(r)];
-        cost = std::max<int64_t>(cost, int64_t(bands(k)) * steps(k));
+      while (r < e && r - q < per && ps.s_g[size_t(r)] == G) {
+        cost = std::max<int64_t>(cost, ps.s_cost[size_t(r)]);
         ++r;
       }
       wt.push_back(make_int2(int32_t(q), (G << 16) | int32_t(r - q)));

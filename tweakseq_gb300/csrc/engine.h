@@ -79,7 +79,12 @@ struct SortRec {
 struct PlanScratch {
   std::vector<int8_t> lsel;
   std::vector<int32_t> gsel, rsel, order;
+  std::vector<int64_t> cost;  // bands x steps per pair
   std::vector<SortRec> recs, tmp;
+  // The same per pair, gathered into sorted order.
+  std::vector<int8_t> s_lt;
+  std::vector<int32_t> s_g, s_cols;
+  std::vector<int64_t> s_cost;
 };
 
 bool tune_table_loaded();

@@ -1,4 +1,8 @@
 // fill_cta.cu -- instantiations of the CTA-per-pair int32 fill.
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "fill_cta.cuh"
 
 namespace tsq {
@@ -28,15 +32,29 @@ int occ(bool local) {
 
 }  // namespace fill
 
+// Resident CTAs of the long-pair fill on the current device (occupancy
+// queries cached per device and kernel, as for the warp fills).
 int cta_blocks(int out_mode, bool local) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int>, int> known;
+  const auto key = std::make_tuple(dev, out_mode, int(local));
+  {
+    std::lock_guard<std::mutex> g(mu);
+    const auto it = known.find(key);
+    if (it != known.end()) return it->second;
+  }
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int per_sm = 0;
   switch (out_mode) {
     case kOutScore: per_sm = fill::occ<kOutScore>(local); break;
     case kOutIdent: per_sm = fill::occ<kOutIdent>(local); break;
     case kOutTrace: per_sm = fill::occ<kOutTrace>(local); break;
+  }
+  if (per_sm * sms > 0) {
+    std::lock_guard<std::mutex> g(mu);
+    known[key] = per_sm * sms;
   }
   return per_sm * sms;
 }

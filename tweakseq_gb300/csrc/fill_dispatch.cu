@@ -1,4 +1,8 @@
 // fill_dispatch.cu -- picks the fill kernel for an output mode and lane type.
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "fill_i16.cuh"
 #include "fill_i32.cuh"
 
@@ -36,7 +40,34 @@ bool shape_supported(const Shape &sh, int out_mode, bool local) {
   return sh.G == 4 || sh.G == 8 || sh.G == 16 || sh.G == 32;
 }
 
+namespace {
+int fill_blocks_uncached(int R, int i16, int out_mode, bool local);
+}
+
+// Resident blocks of a fill launch on the current device.  The occupancy
+// queries (and the shared-memory attribute they set) cost far more than a
+// plan's host work, so each answer is kept per device and kernel.
 int fill_blocks(int R, int i16, int out_mode, bool local) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int, int>, int> known;
+  const auto key = std::make_tuple(dev, R, i16, out_mode, int(local));
+  {
+    std::lock_guard<std::mutex> g(mu);
+    const auto it = known.find(key);
+    if (it != known.end()) return it->second;
+  }
+  const int v = fill_blocks_uncached(R, i16, out_mode, local);
+  if (v > 0) {
+    std::lock_guard<std::mutex> g(mu);
+    known[key] = v;
+  }
+  return v;
+}
+
+namespace {
+int fill_blocks_uncached(int R, int i16, int out_mode, bool local) {
   if (R != 8) return 0;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -51,6 +82,7 @@ int fill_blocks(int R, int i16, int out_mode, bool local) {
   }
   return per_sm * sms;
 }
+}  // namespace
 
 cudaError_t launch_fill(int R, int i16, int out_mode, bool local, const FillArgs &a, int blocks,
                         cudaStream_t st) {
