@@ -331,3 +331,44 @@ def test_alignment_batch_in_waves(monkeypatch):
     assert big.any() and (~big).any()
     assert np.all(raw["status"][big] == N.E_TOO_LARGE) and np.all(raw["status"][~big] == 0)
     N.lib().tsq_results_free(raw.ctypes.data, len(raw))
+
+
+@pytest.mark.parametrize("output,local", [("score", False), ("identity", False), ("score", True)])
+def test_chunked_call_equals_single_plan(output, local):
+    """A large score or identity call through tsq_align_batch runs in chunks
+    planned while earlier chunks run; every result equals the single-plan
+    device-resident batch's, and a sample equals the oracle's."""
+    ps = W.uneven_pairs(n_pairs=40000, seed=12)
+    mode = "local" if local else "global"
+    got = A.align_batch(ps, output=output, mode=mode)
+    with A.Batch(ps, output=output, mode=mode, use_graph=False) as b:
+        b.run()
+        want = b.results()
+    for f in ("score", "a_begin", "a_end", "b_begin", "b_end", "n_ident", "n_cols", "status"):
+        assert np.array_equal(got.table[f], want.table[f]), f
+    idx = np.random.default_rng(5).choice(len(ps), 300, replace=False)
+    sub = ps.subset(idx)
+    o = O.batch(sub.seqs, sub.a_off, sub.a_len, sub.b_off, sub.b_len, O.BLOSUM62, 11, 1, local,
+                O.MODE_IDENT if output == "identity" else O.MODE_SCORE)
+    assert np.array_equal(got.table["score"][idx], o["score"])
+    if output == "identity":
+        assert np.array_equal(got.table["n_ident"][idx], o["n_ident"])
+        assert np.array_equal(got.table["n_cols"][idx], o["n_cols"])
+    if local:
+        assert np.array_equal(got.table["a_end"][idx], o["a_end"])
+        assert np.array_equal(got.table["b_end"][idx], o["b_end"])
+
+
+def test_chunked_call_reports_the_first_bad_pair():
+    ps = W.uneven_pairs(n_pairs=40000, seed=13)
+    seqs, tab = A._as_inputs(ps)
+    tab = tab.copy()
+    tab["a_len"][30000] = -1  # in the third chunk
+    raw = np.zeros(len(tab), dtype=N.RESULT_DTYPE)
+    p, keep = N.make_params(output="score")
+    rc = N.lib().tsq_align_batch(seqs.ctypes.data, len(seqs), tab.ctypes.data, len(tab), ctypes.byref(p),
+                                 ctypes.byref(A._opts()), raw.ctypes.data)
+    assert rc == N.E_INVALID_ARG
+    # The engines are usable again afterwards.
+    ok = A.align_batch(ps.subset(np.arange(40000)), output="score")
+    assert (ok.table["status"] == 0).all()

@@ -16,8 +16,14 @@ namespace {
 struct ThreadCache {
   std::unique_ptr<tsq_batch> pair_engine;
   std::unique_ptr<tsq_batch> batch_engine;
+  std::vector<std::unique_ptr<tsq_batch>> chunk_engines;  // chunks 1.. of a large call
   int pair_dev = -1, batch_dev = -1;
 };
+
+// A score or identity call of at least 2 * kChunkPairs pairs runs as up to
+// kMaxChunks chunks (see align_in_chunks).
+constexpr int64_t kChunkPairs = 16384;
+constexpr int kMaxChunks = 4;
 
 ThreadCache &cache() {
   thread_local ThreadCache c;
@@ -42,6 +48,42 @@ int guarded(F &&f) {
   } catch (...) {
     return TSQ_E_CUDA;
   }
+}
+
+// A large score or identity call runs as a few chunks of consecutive pairs,
+// each planned by its own batch object and run on its own stream: chunk k+1
+// is planned on the host while chunk k runs, the residues go up and are
+// encoded once (by chunk 0), and the chunks' persistent launches fill each
+// other's tails on the device.  Each pair's result does not depend on the
+// chunking.
+int align_in_chunks(ThreadCache &c, tsq_batch *e, const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *pairs,
+                    int64_t n, const tsq_params *p, const tsq_batch_opts *opts, tsq_result *out) {
+  const int K = int(std::min<int64_t>(kMaxChunks, n / kChunkPairs));
+  while (int(c.chunk_engines.size()) < K - 1) c.chunk_engines.emplace_back(new tsq_batch());
+  std::vector<tsq_batch *> eng(static_cast<size_t>(K));
+  eng[0] = e;
+  for (int k = 1; k < K; ++k) eng[size_t(k)] = c.chunk_engines[size_t(k - 1)].get();
+  auto begin = [&](int k) { return n * k / K; };
+  const tsq_batch_opts o{opts ? opts->device : -1, 0, opts ? opts->autotune : 0, 0};
+  int64_t cells = 0;
+  for (int64_t k = 0; k < n; ++k) cells += int64_t(std::max(pairs[k].a_len, 0)) * std::max(pairs[k].b_len, 0);
+  int launched = 0, rc = TSQ_OK;
+  for (int k = 0; k < K && rc == TSQ_OK; ++k) {
+    const tsq_pair_desc *pk = pairs + begin(k);
+    const int64_t nk = begin(k + 1) - begin(k);
+    rc = tsq::batch_plan_chunk(eng[size_t(k)], k == 0 ? nullptr : e, seqs, seqs_len, pk, nk, p, &o, n, cells);
+    if (rc == TSQ_OK) rc = tsq::batch_run_async(eng[size_t(k)]);
+    if (rc == TSQ_OK) ++launched;
+  }
+  int status = rc;
+  for (int k = 0; k < launched; ++k) {
+    const int sync_rc = tsq::batch_sync(eng[size_t(k)]);
+    if (status != TSQ_OK && status != TSQ_E_INVALID_RESIDUE) continue;  // drain the rest, report the first error
+    int r = sync_rc;
+    if (r == TSQ_OK) r = tsq::batch_results(eng[size_t(k)], out + begin(k));
+    if (r != TSQ_OK && (status == TSQ_OK || r != TSQ_E_INVALID_RESIDUE)) status = r;
+  }
+  return status;
 }
 
 // Runs an alignment batch wave by wave (see tsq_align_batch).
@@ -175,6 +217,8 @@ int tsq_align_batch(const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *
       }
       if (total > budget) return align_in_waves(e, seqs, seqs_len, pairs, n, p, opts, out, bytes, budget);
     }
+    if (p && p->output != TSQ_OUT_ALIGNMENT && n >= 2 * kChunkPairs && pairs)
+      return align_in_chunks(c, e, seqs, seqs_len, pairs, n, p, opts, out);
     int rc = tsq::batch_plan(e, seqs, seqs_len, pairs, n, p, opts, false);
     if (rc) return rc;
     if ((rc = tsq::batch_run_async(e))) return rc;

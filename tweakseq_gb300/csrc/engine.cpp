@@ -12,6 +12,10 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
 #include <numeric>
 #include <thread>
 
@@ -81,24 +85,98 @@ constexpr int kR = 8;
 // Longest sequence the int32 kernels take: coordinates travel in 20 bits.
 constexpr int64_t kMaxLen = (1 << 20) - 1;
 
-// Runs f(begin, end, slot) over [0, n) on up to 8 host threads (slot =
-// 0..threads-1), one thread when n is small.  Returns the thread count.
+// A small pool of host worker threads for the planner's per-pair passes,
+// started on first use and kept for the life of the process (spawning
+// threads per plan costs as much as the work).  One job at a time: a caller
+// that finds the pool busy runs its job alone.
+class WorkerPool {
+ public:
+  static WorkerPool &get() {
+    static WorkerPool pool;
+    return pool;
+  }
+  int workers() const { return int(threads_.size()); }
+  // Runs task(i) for i in [0, tasks) on the workers and the calling thread.
+  // False (nothing run) when another job holds the pool.
+  bool run(int tasks, const std::function<void(int)> &task) {
+    std::unique_lock<std::mutex> busy(busy_, std::try_to_lock);
+    if (!busy.owns_lock()) return false;
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      task_ = &task;
+      tasks_ = tasks;
+      next_.store(0);
+      left_ = tasks;
+      ++gen_;
+    }
+    cv_.notify_all();
+    work();
+    std::unique_lock<std::mutex> g(mu_);
+    done_.wait(g, [&] { return left_ == 0; });
+    task_ = nullptr;
+    return true;
+  }
+
+ private:
+  WorkerPool() {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int n = int(std::min(7u, hw > 1 ? hw - 1 : 0u));
+    for (int i = 0; i < n; ++i) threads_.emplace_back([this] { loop(); });
+  }
+  ~WorkerPool() {
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (std::thread &t : threads_) t.join();
+  }
+  void work() {
+    for (;;) {
+      const int i = next_.fetch_add(1);
+      if (i >= tasks_) return;
+      (*task_)(i);
+      std::lock_guard<std::mutex> g(mu_);
+      if (--left_ == 0) done_.notify_all();
+    }
+  }
+  void loop() {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> g(mu_);
+        cv_.wait(g, [&] { return stop_ || gen_ != seen; });
+        if (stop_) return;
+        seen = gen_;
+      }
+      work();
+    }
+  }
+  std::vector<std::thread> threads_;
+  std::mutex busy_, mu_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)> *task_ = nullptr;
+  int tasks_ = 0, left_ = 0;
+  std::atomic<int> next_{0};
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+};
+
+// Runs f(begin, end, slot) over [0, n) in up to 8 slices (slot = slice
+// number) on the worker pool; one slice when n is small or the pool is busy.
 template <class F>
 int parallel_for(int64_t n, F &&f) {
-  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const int threads = int(std::min<int64_t>({8, int64_t(hw), std::max<int64_t>(1, n / 16384)}));
-  if (threads <= 1) {
-    f(int64_t(0), n, 0);
-    return 1;
+  WorkerPool &pool = WorkerPool::get();
+  const int slices = int(std::min<int64_t>({8, int64_t(pool.workers()) + 1, std::max<int64_t>(1, n / 4096)}));
+  if (slices > 1) {
+    const int64_t chunk = (n + slices - 1) / slices;
+    const std::function<void(int)> task = [&](int i) {
+      f(std::min(n, i * chunk), std::min(n, (i + 1) * chunk), i);
+    };
+    if (pool.run(slices, task)) return slices;
   }
-  const int64_t chunk = (n + threads - 1) / threads;
-  std::vector<std::thread> th;
-  th.reserve(size_t(threads - 1));
-  for (int i = 1; i < threads; ++i)
-    th.emplace_back([&f, i, chunk, n] { f(std::min(n, i * chunk), std::min(n, (i + 1) * chunk), i); });
-  f(int64_t(0), std::min(n, chunk), 0);
-  for (std::thread &x : th) x.join();
-  return threads;
+  f(int64_t(0), n, 0);
+  return 1;
 }
 
 // Stable LSD radix sort by key (ascending) in 11-bit digits over the low
@@ -162,6 +240,7 @@ tsq_batch::~tsq_batch() {
   if (ev_fetch) cudaEventDestroy(ev_fetch);
   if (ev_fork) cudaEventDestroy(ev_fork);
   if (ev_join) cudaEventDestroy(ev_join);
+  if (ev_encoded) cudaEventDestroy(ev_encoded);
   if (side) cudaStreamDestroy(side);
   if (gexec) cudaGraphExecDestroy(gexec);
   if (graph) cudaGraphDestroy(graph);
@@ -172,11 +251,34 @@ tsq_batch::~tsq_batch() {
 
 namespace tsq {
 
+namespace {
+int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t seqs_len,
+              const tsq_pair_desc *pairs, int64_t n, const tsq_params *p, const tsq_batch_opts *opts, bool plain,
+              int64_t call_pairs, int64_t call_cells);
+}  // namespace
+
 int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *pairs, int64_t n,
                const tsq_params *p, const tsq_batch_opts *opts, bool plain) {
+  return plan_impl(b, nullptr, seqs, seqs_len, pairs, n, p, opts, plain, 0, 0);
+}
+
+int batch_plan_chunk(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t seqs_len,
+                     const tsq_pair_desc *pairs, int64_t n, const tsq_params *p, const tsq_batch_opts *opts,
+                     int64_t call_pairs, int64_t call_cells) {
+  if (!b || owner == b || call_pairs < n || call_cells < 0) return TSQ_E_INVALID_ARG;
+  if (!owner) return plan_impl(b, nullptr, seqs, seqs_len, pairs, n, p, opts, false, call_pairs, call_cells);
+  const tsq_batch_opts o{owner->device, 0, opts ? opts->autotune : 0, 0};
+  return plan_impl(b, owner, nullptr, owner->seqs_len, pairs, n, p, &o, false, call_pairs, call_cells);
+}
+
+namespace {
+int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t seqs_len,
+              const tsq_pair_desc *pairs, int64_t n, const tsq_params *p, const tsq_batch_opts *opts, bool plain,
+              int64_t call_pairs, int64_t call_cells) {
   if (!b || !p || n < 0 || seqs_len < 0) return TSQ_E_INVALID_ARG;
+  b->input_owner = owner;
   if (n > 0 && !pairs) return TSQ_E_INVALID_ARG;
-  if (seqs_len > 0 && !seqs) return TSQ_E_INVALID_ARG;
+  if (seqs_len > 0 && !seqs && !owner) return TSQ_E_INVALID_ARG;
   if (n > INT32_MAX / 2) return TSQ_E_TOO_LARGE;
   if (p->gap_open < 0 || p->gap_extend < 0 || p->gap_open > 1000000 || p->gap_extend > 1000000)
     return TSQ_E_INVALID_ARG;
@@ -215,6 +317,7 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   if (!b->ev_join) TSQ_TRY(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
   for (auto &e : b->ev)
     if (!e) TSQ_TRY(cudaEventCreate(&e));
+  if (!b->ev_encoded) TSQ_TRY(cudaEventCreateWithFlags(&b->ev_encoded, cudaEventDisableTiming));
 
   b->scheme = sc;
   b->params = *p;
@@ -287,13 +390,16 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
 
   // The residues go up first, so the copy overlaps the planning below.  Any
   // return from here on waits for it: the caller's buffer must outlive it.
-  TSQ_TRY(b->seqs.ensure(size_t(seqs_len) + 128));
-  TSQ_TRY(b->codes.ensure(size_t(seqs_len) + 128));
+  // (A chunk of a larger call uses its first chunk's residues instead.)
   struct SyncOnExit {
     cudaStream_t st;
     ~SyncOnExit() { cudaStreamSynchronize(st); }
   } sync_on_exit{b->stream};
-  if (seqs_len > 0) TSQ_TRY(cudaMemcpyAsync(b->seqs.p, seqs, size_t(seqs_len), cudaMemcpyHostToDevice, b->stream));
+  if (!b->input_owner) {
+    TSQ_TRY(b->seqs.ensure(size_t(seqs_len) + 128));
+    TSQ_TRY(b->codes.ensure(size_t(seqs_len) + 128));
+    if (seqs_len > 0) TSQ_TRY(cudaMemcpyAsync(b->seqs.p, seqs, size_t(seqs_len), cudaMemcpyHostToDevice, b->stream));
+  }
 
   // ---- lane types, shapes and order (one parallel pass over the pairs) ----
   // Score fills run in int16x2 when the pair's values provably fit: the
@@ -319,10 +425,14 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   ch.out_mode = b->out_mode;
   ch.local = b->local;
   ch.sms = sms;
-  ch.npairs = plain ? 1 : n;
+  // Shapes follow the whole call's size (a chunk's pairs get the lane widths
+  // a single plan would give them).
+  const int64_t shape_pairs = call_pairs > 0 ? call_pairs : n;
+  const int64_t shape_cells = call_pairs > 0 ? call_cells : cells;
+  ch.npairs = plain ? 1 : shape_pairs;
   if (!plain) {
     const double lanes = double(sms) * 24.0 * 32.0;
-    ch.avg_lane_steps = double(cells) / (lanes * kR);
+    ch.avg_lane_steps = double(shape_cells) / (lanes * kR);
   }
   ch.use_table = b->autotune && tune_table_loaded();
   PlanScratch &ps = b->scratch;
@@ -352,7 +462,7 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   std::vector<ShapePart> sparts(8);
   {
     const double lanes = double(sms) * 24.0 * 32.0;
-    const double cta_budget = std::max(20000.0, plain ? 0.0 : double(cells) / (lanes * kR));
+    const double cta_budget = std::max(20000.0, plain ? 0.0 : double(shape_cells) / (lanes * kR));
     const int64_t go = p->gap_open, ge = p->gap_extend;
     const bool try16 = b->out_mode == kOutScore && p->lane != TSQ_LANE_I32;
     const int64_t smax = std::max(sc.max_score, 0), sneg = std::max<int64_t>(0, -int64_t(sc.min_score));
@@ -611,8 +721,16 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
   TSQ_TRY(cudaStreamSynchronize(st));
   return TSQ_OK;
 }
+}  // namespace
 
 namespace {
+
+const uint8_t *seqs_dev(const tsq_batch *b) {
+  return b->input_owner ? b->input_owner->seqs.as<uint8_t>() : b->seqs.as<uint8_t>();
+}
+const uint8_t *codes_dev(const tsq_batch *b) {
+  return b->input_owner ? b->input_owner->codes.as<uint8_t>() : b->codes.as<uint8_t>();
+}
 
 // Inside stream capture an event record becomes an external event-record
 // node, so the event can still be timed after each graph launch.
@@ -626,7 +744,13 @@ int enqueue_run(tsq_batch *b) {
   const int nl = int(b->launches.size());
   TSQ_TRY(cudaMemsetAsync(b->counters.p, 0, sizeof(int32_t) * (size_t(nl) + 2), st));
   TSQ_TRY(record(b, 0));
-  TSQ_TRY(launch_encode(b->seqs.as<uint8_t>(), b->seqs_len, b->lut.as<uint8_t>(), b->codes.as<uint8_t>(), st));
+  if (b->input_owner) {
+    // The owner encodes the residues on its stream.
+    TSQ_TRY(cudaStreamWaitEvent(st, b->input_owner->ev_encoded, 0));
+  } else {
+    TSQ_TRY(launch_encode(b->seqs.as<uint8_t>(), b->seqs_len, b->lut.as<uint8_t>(), b->codes.as<uint8_t>(), st));
+    if (!b->capturing) TSQ_TRY(cudaEventRecord(b->ev_encoded, st));
+  }
   TSQ_TRY(record(b, 1));
   int32_t *rerun_count = b->counters.as<int32_t>() + nl + 1;
   // The CTA launch (long pairs) runs on a side stream next to the others.
@@ -640,7 +764,7 @@ int enqueue_run(tsq_batch *b) {
     const Launch &L = b->launches[size_t(l)];
     if (L.cta) {
       FillArgs a{};
-      a.codes = b->codes.as<uint8_t>();
+      a.codes = codes_dev(b);
       a.pairs = b->pairs.as<PairDev>();
       a.tasks = b->tasks.as<int32_t>() + L.task_begin;
       a.n_wtasks = L.n_wtasks;
@@ -664,7 +788,7 @@ int enqueue_run(tsq_batch *b) {
                                       b->rerun_tasks.as<int32_t>(), b->rerun_wtasks.as<int2>(), rerun_count, st));
     }
     FillArgs a{};
-    a.codes = b->codes.as<uint8_t>();
+    a.codes = codes_dev(b);
     a.pairs = b->pairs.as<PairDev>();
     a.tasks = L.rerun ? b->rerun_tasks.as<int32_t>() : b->tasks.as<int32_t>();
     a.wtasks = L.rerun ? b->rerun_wtasks.as<int2>() : b->wtasks.as<int2>() + L.wt_begin;
@@ -692,8 +816,8 @@ int enqueue_run(tsq_batch *b) {
   TSQ_TRY(record(b, 2));
   if (b->out_mode == kOutTrace) {
     WalkArgs w{};
-    w.seqs = b->seqs.as<uint8_t>();
-    w.codes = b->codes.as<uint8_t>();
+    w.seqs = seqs_dev(b);
+    w.codes = codes_dev(b);
     w.pairs = b->pairs.as<PairDev>();
     w.tasks = b->tasks.as<int32_t>();
     w.n_tasks = int32_t(b->n);

@@ -118,6 +118,11 @@ struct tsq_batch {
   std::vector<int64_t> aln_off_h;
   int64_t aln_bytes = 0;
   bool has_run = false;
+  // Chunk of a larger call: the residues and their codes live in another
+  // batch object (the call's first chunk), which uploads and encodes them;
+  // this object's fills wait on that object's ev_encoded.
+  const tsq_batch *input_owner = nullptr;
+  cudaEvent_t ev_encoded = nullptr;  // recorded after this object's encode
 
   tsq::DevBuf seqs, codes, pairs, tasks, wtasks, res, bnd, planes, plane_off, aln, aln_off, shape_g, shape_r, counters,
       lut, matrix, overflow, rerun_tasks, rerun_wtasks;
@@ -135,6 +140,14 @@ struct tsq_batch {
 namespace tsq {
 int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *pairs, int64_t n,
                const tsq_params *p, const tsq_batch_opts *opts, bool plain);
+// Plans one chunk of a larger call.  The first chunk (owner == nullptr)
+// uploads and encodes the residues; later chunks use the owner's, and
+// their pair offsets refer to them.  call_pairs / call_cells are the whole
+// call's totals, so that every pair gets the lane width a single plan of the
+// call would give it.
+int batch_plan_chunk(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t seqs_len,
+                     const tsq_pair_desc *pairs, int64_t n, const tsq_params *p, const tsq_batch_opts *opts,
+                     int64_t call_pairs, int64_t call_cells);
 int batch_run_async(tsq_batch *b);
 int batch_sync(tsq_batch *b);
 int batch_results(tsq_batch *b, tsq_result *out);
