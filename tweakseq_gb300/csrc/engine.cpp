@@ -395,9 +395,12 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
     cudaStream_t st;
     ~SyncOnExit() { cudaStreamSynchronize(st); }
   } sync_on_exit{b->stream};
+  // Score batches also get class codes for the int16x2 fill.
+  b->classes = b->out_mode == kOutScore && p->lane != TSQ_LANE_I32;
   if (!b->input_owner) {
     TSQ_TRY(b->seqs.ensure(size_t(seqs_len) + 128));
     TSQ_TRY(b->codes.ensure(size_t(seqs_len) + 128));
+    if (b->classes) TSQ_TRY(b->ccodes.ensure(size_t(seqs_len) + 128));
     if (seqs_len > 0) TSQ_TRY(cudaMemcpyAsync(b->seqs.p, seqs, size_t(seqs_len), cudaMemcpyHostToDevice, b->stream));
   }
 
@@ -610,7 +613,7 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
     L.wt_begin = int32_t(wt_all.size());
     L.n_wtasks = int32_t(wt.size());
     for (int32_t w : worder) wt_all.push_back(wt[size_t(w)]);
-    const int max_blocks = fill_blocks(L.R, L.i16, b->out_mode, b->local);
+    const int max_blocks = fill_blocks(L.R, L.i16, b->out_mode, b->local, sc.nclasses);
     if (max_blocks <= 0) return TSQ_E_CUDA;
     const int warps_per_block = fill_threads_for(L.i16) / 32;
     const int64_t needed = (int64_t(L.n_wtasks) + warps_per_block - 1) / warps_per_block;
@@ -691,6 +694,10 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   TSQ_TRY(b->rerun_h.ensure(sizeof(int32_t)));
   TSQ_TRY(b->lut.ensure(256));
   TSQ_TRY(b->matrix.ensure(kLetters * kLetters));
+  if (b->classes) {
+    TSQ_TRY(b->clut.ensure(256));
+    TSQ_TRY(b->cmatrix.ensure(kLetters * kLetters));
+  }
   TSQ_TRY(b->res_h.ensure(sizeof(ResultDev) * size_t(n)));
   if (b->out_mode == kOutTrace) {
     TSQ_TRY(b->planes.ensure(size_t(plane_total)));
@@ -708,6 +715,13 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   }
   TSQ_TRY(cudaMemcpyAsync(b->lut.p, lut, 256, cudaMemcpyHostToDevice, st));
   TSQ_TRY(cudaMemcpyAsync(b->matrix.p, sc.score, kLetters * kLetters, cudaMemcpyHostToDevice, st));
+  uint8_t clut[256];
+  if (b->classes) {
+    build_class_lut(sc, clut);
+    TSQ_TRY(cudaMemcpyAsync(b->clut.p, clut, 256, cudaMemcpyHostToDevice, st));
+    TSQ_TRY(cudaMemcpyAsync(b->cmatrix.p, sc.cscore, size_t(sc.nclasses) * sc.nclasses, cudaMemcpyHostToDevice,
+                            st));
+  }
   if (b->out_mode == kOutTrace && n > 0) {
     TSQ_TRY(cudaMemcpyAsync(b->plane_off.p, ploff.data(), sizeof(int64_t) * size_t(n), cudaMemcpyHostToDevice, st));
     TSQ_TRY(cudaMemcpyAsync(b->aln_off.p, b->aln_off_h.data(), sizeof(int64_t) * size_t(n), cudaMemcpyHostToDevice,
@@ -731,6 +745,9 @@ const uint8_t *seqs_dev(const tsq_batch *b) {
 const uint8_t *codes_dev(const tsq_batch *b) {
   return b->input_owner ? b->input_owner->codes.as<uint8_t>() : b->codes.as<uint8_t>();
 }
+const uint8_t *ccodes_dev(const tsq_batch *b) {
+  return b->input_owner ? b->input_owner->ccodes.as<uint8_t>() : b->ccodes.as<uint8_t>();
+}
 
 // Inside stream capture an event record becomes an external event-record
 // node, so the event can still be timed after each graph launch.
@@ -748,7 +765,9 @@ int enqueue_run(tsq_batch *b) {
     // The owner encodes the residues on its stream.
     TSQ_TRY(cudaStreamWaitEvent(st, b->input_owner->ev_encoded, 0));
   } else {
-    TSQ_TRY(launch_encode(b->seqs.as<uint8_t>(), b->seqs_len, b->lut.as<uint8_t>(), b->codes.as<uint8_t>(), st));
+    TSQ_TRY(launch_encode(b->seqs.as<uint8_t>(), b->seqs_len, b->lut.as<uint8_t>(), b->codes.as<uint8_t>(),
+                          b->classes ? b->clut.as<uint8_t>() : nullptr, b->classes ? b->ccodes.as<uint8_t>() : nullptr,
+                          st));
     if (!b->capturing) TSQ_TRY(cudaEventRecord(b->ev_encoded, st));
   }
   TSQ_TRY(record(b, 1));
@@ -805,6 +824,11 @@ int enqueue_run(tsq_batch *b) {
     a.plane_off = b->plane_off.as<int64_t>();
     a.overflow = b->overflow.as<int32_t>();
     a.max_score = b->scheme.max_score;
+    if (L.i16) {
+      a.ccodes = ccodes_dev(b);
+      a.cmatrix = b->cmatrix.as<int8_t>();
+      a.nclasses = b->scheme.nclasses;
+    }
     TSQ_TRY(launch_fill(L.R, L.i16, b->out_mode, b->local, a, L.blocks, st));
   }
   if (forked) {
@@ -962,7 +986,8 @@ int batch_results(tsq_batch *b, tsq_result *out) {
 int64_t batch_device_bytes(const tsq_batch *b) {
   const tsq::DevBuf *bufs[] = {&b->seqs, &b->codes, &b->pairs, &b->tasks, &b->wtasks, &b->res, &b->bnd,
                                &b->planes, &b->plane_off, &b->aln, &b->aln_off, &b->shape_g, &b->shape_r,
-                               &b->counters, &b->lut, &b->matrix, &b->overflow, &b->rerun_tasks, &b->rerun_wtasks};
+                               &b->counters, &b->lut, &b->matrix, &b->overflow, &b->rerun_tasks, &b->rerun_wtasks,
+                               &b->ccodes, &b->clut, &b->cmatrix};
   int64_t total = 0;
   for (const tsq::DevBuf *d : bufs) total += int64_t(d->cap);
   return total;

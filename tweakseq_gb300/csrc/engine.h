@@ -126,6 +126,9 @@ struct tsq_batch {
 
   tsq::DevBuf seqs, codes, pairs, tasks, wtasks, res, bnd, planes, plane_off, aln, aln_off, shape_g, shape_r, counters,
       lut, matrix, overflow, rerun_tasks, rerun_wtasks;
+  // Score classes for the int16x2 fill (score output only).
+  tsq::DevBuf ccodes, clut, cmatrix;
+  bool classes = false;
   tsq::PinBuf res_h, aln_h, rerun_h;
   int64_t n_checked = 0;
   int32_t checked_begin = 0;

@@ -14,13 +14,13 @@ template <int OUT>
 int occupancy_i32(bool local, size_t smem);
 cudaError_t launch_i16(bool check, bool local, const FillArgs &a, int blocks, size_t smem, cudaStream_t st);
 int occupancy_i16(bool check, bool local, size_t smem);
-size_t smem_i16();
+size_t smem_i16(int nclasses);
 }  // namespace fill
 
 int fill_threads() { return fill::kThreads; }
 
-size_t fill_smem_bytes(int R, int i16, int out_mode) {
-  if (i16) return fill::smem_i16();
+size_t fill_smem_bytes(int R, int i16, int out_mode, int nclasses) {
+  if (i16) return fill::smem_i16(nclasses);
   const size_t top = out_mode == kOutIdent ? 16 : 8;
   return size_t(fill::kMatBytes) + size_t(kLetters) * fill::kThreads * size_t(R) +
          size_t(fill::kSlotsPerBlock) * (fill::kTopRing * top + fill::kCodeRing + 2 * fill::kRingPad);
@@ -41,24 +41,24 @@ bool shape_supported(const Shape &sh, int out_mode, bool local) {
 }
 
 namespace {
-int fill_blocks_uncached(int R, int i16, int out_mode, bool local);
+int fill_blocks_uncached(int R, int i16, int out_mode, bool local, int nclasses);
 }
 
 // Resident blocks of a fill launch on the current device.  The occupancy
 // queries (and the shared-memory attribute they set) cost far more than a
 // plan's host work, so each answer is kept per device and kernel.
-int fill_blocks(int R, int i16, int out_mode, bool local) {
+int fill_blocks(int R, int i16, int out_mode, bool local, int nclasses) {
   int dev = 0;
   cudaGetDevice(&dev);
   static std::mutex mu;
-  static std::map<std::tuple<int, int, int, int, int>, int> known;
-  const auto key = std::make_tuple(dev, R, i16, out_mode, int(local));
+  static std::map<std::tuple<int, int, int, int, int, int>, int> known;
+  const auto key = std::make_tuple(dev, R, i16, out_mode, int(local), i16 ? nclasses : 0);
   {
     std::lock_guard<std::mutex> g(mu);
     const auto it = known.find(key);
     if (it != known.end()) return it->second;
   }
-  const int v = fill_blocks_uncached(R, i16, out_mode, local);
+  const int v = fill_blocks_uncached(R, i16, out_mode, local, nclasses);
   if (v > 0) {
     std::lock_guard<std::mutex> g(mu);
     known[key] = v;
@@ -67,12 +67,12 @@ int fill_blocks(int R, int i16, int out_mode, bool local) {
 }
 
 namespace {
-int fill_blocks_uncached(int R, int i16, int out_mode, bool local) {
+int fill_blocks_uncached(int R, int i16, int out_mode, bool local, int nclasses) {
   if (R != 8) return 0;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t smem = fill_smem_bytes(R, i16, out_mode);
+  const size_t smem = fill_smem_bytes(R, i16, out_mode, nclasses);
   if (i16) return out_mode == kOutScore ? fill::occupancy_i16(i16 == 2, local, smem) * sms : 0;
   int per_sm = 0;
   switch (out_mode) {
@@ -87,7 +87,7 @@ int fill_blocks_uncached(int R, int i16, int out_mode, bool local) {
 cudaError_t launch_fill(int R, int i16, int out_mode, bool local, const FillArgs &a, int blocks,
                         cudaStream_t st) {
   if (R != 8) return cudaErrorInvalidValue;
-  const size_t smem = fill_smem_bytes(R, i16, out_mode);
+  const size_t smem = fill_smem_bytes(R, i16, out_mode, i16 ? a.nclasses : kLetters);
   if (i16) {
     if (out_mode != kOutScore) return cudaErrorInvalidValue;
     return fill::launch_i16(i16 == 2, local, a, blocks, smem, st);

@@ -1,5 +1,7 @@
 // fill_i16.cu -- the int16x2 score fills (plain and overflow-checked) and
 // the overflow collector of the int32 re-run.
+#include <algorithm>
+
 #include "fill_i16.cuh"
 
 namespace tsq {
@@ -22,17 +24,23 @@ cudaError_t launch_i16(bool check, bool local, const FillArgs &args, int blocks,
   return cudaGetLastError();
 }
 
+size_t smem_i16(int nclasses);
+
 int occupancy_i16(bool check, bool local, size_t smem) {
   auto k = check ? (local ? fill_i16_kernel<true, true> : fill_i16_kernel<false, true>)
                  : (local ? fill_i16_kernel<true, false> : fill_i16_kernel<false, false>);
-  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return 0;
+  // The attribute allows the largest profile (26 classes), so that every
+  // scheme's launch fits whatever scheme was sized first.
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(std::max(smem, smem_i16(kLetters)))) !=
+      cudaSuccess)
+    return 0;
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kThreads16, smem) != cudaSuccess) return 0;
   return nb;
 }
 
-size_t smem_i16() {
-  return size_t(kMatBytes) + size_t(2 * kLetters) * kThreads16 * sizeof(uint2) +
+size_t smem_i16(int nclasses) {
+  return size_t(kMatBytes) + size_t(2 * nclasses) * kThreads16 * sizeof(uint2) +
          size_t(kSlots16) * (kTopRing * sizeof(uint32_t) + kCodeRing16 + 2 * kRingPad);
 }
 

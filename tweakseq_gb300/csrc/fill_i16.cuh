@@ -126,19 +126,21 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
   const bool have = gw < count;
   const int pid = have ? A.tasks[begin + gw] : 0;
   int m = 0, n = 0;
-  const uint8_t *qa_codes = A.codes;
+  // Residues as score classes (the profile is indexed by class).
+  const int ncls = A.nclasses;
+  const uint8_t *qa_codes = A.ccodes;
   int64_t boff = 0;
   if (have) {
     const PairDev pr = A.pairs[pid];
     m = pr.a_len;
     n = pr.b_len;
-    qa_codes = A.codes + pr.a_off;
+    qa_codes = A.ccodes + pr.a_off;
     boff = pr.b_off;
   }
-  const uint8_t *qb_codes = A.codes + boff;
+  const uint8_t *qb_codes = A.ccodes + boff;
   bool bad = false;
-  for (int k = t; k < m; k += G) bad |= qa_codes[k] >= kLetters;
-  for (int k = t; k < n; k += G) bad |= qb_codes[k] >= kLetters;
+  for (int k = t; k < m; k += G) bad |= qa_codes[k] >= ncls;
+  for (int k = t; k < n; k += G) bad |= qb_codes[k] >= ncls;
   const unsigned gm = group_mask_rt(lane, G);
   const bool gbad = (__ballot_sync(0xffffffffu, bad) & gm) != 0;
   const bool trivial = (m == 0 || n == 0 || gbad);
@@ -174,7 +176,7 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
         qb[r] = (gact && rowB + r < m) ? int(qa_codes[rowB + r]) : -1;
       }
 #pragma unroll 2
-      for (int c = 0; c < kLetters; ++c) {
+      for (int c = 0; c < ncls; ++c) {
         uint32_t wa[2], wb[2];
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
@@ -182,8 +184,8 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             const int xa = qa[q * 4 + k], xb = qb[q * 4 + k];
-            va |= (xa >= 0 ? uint32_t(uint8_t(s_mat[xa * kLetters + c])) : 0u) << (8 * k);
-            vb |= (xb >= 0 ? uint32_t(uint8_t(s_mat[xb * kLetters + c])) : 0u) << (8 * k);
+            va |= (xa >= 0 ? uint32_t(uint8_t(s_mat[xa * ncls + c])) : 0u) << (8 * k);
+            vb |= (xb >= 0 ? uint32_t(uint8_t(s_mat[xb * ncls + c])) : 0u) << (8 * k);
           }
           wa[q] = va;
           wb[q] = vb;
@@ -208,18 +210,18 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
 
     cp_async_wait_all();
     __syncwarp();
-    stage_chunk_rt<uint32_t, kCodeRing16>(G, 0, t, nact, top, top_ring, A.codes, boff, code_ring);
+    stage_chunk_rt<uint32_t, kCodeRing16>(G, 0, t, nact, top, top_ring, A.ccodes, boff, code_ring);
     cp_async_commit();
     cp_async_wait_all();
     __syncwarp();
-    stage_chunk_rt<uint32_t, kCodeRing16>(G, 1, t, nact, top, top_ring, A.codes, boff, code_ring);
+    stage_chunk_rt<uint32_t, kCodeRing16>(G, 1, t, nact, top, top_ring, A.ccodes, boff, code_ring);
     cp_async_commit();
 
     uint2 pa[2], pb[2];
     uint32_t tv[2];
     {
-      const int ca = min(int(code_ring[(boff - t) & (kCodeRing16 - 1)]), kLetters - 1);
-      const int cb = min(int(code_ring[(boff - t - G) & (kCodeRing16 - 1)]), kLetters - 1);
+      const int ca = min(int(code_ring[(boff - t) & (kCodeRing16 - 1)]), ncls - 1);
+      const int cb = min(int(code_ring[(boff - t - G) & (kCodeRing16 - 1)]), ncls - 1);
       pa[0] = profA[(2 * ca) * kThreads16];
       pb[0] = profB[(2 * cb) * kThreads16];
       tv[0] = top_ring[0];
@@ -244,7 +246,7 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       if (k == 1 && ((s + 1) & (kChunk - 1)) == 0) {
         cp_async_wait_all();
         __syncwarp();
-        stage_chunk_rt<uint32_t, kCodeRing16>(G, (s + 1) / kChunk + 1, t, nact, top, top_ring, A.codes, boff,
+        stage_chunk_rt<uint32_t, kCodeRing16>(G, (s + 1) / kChunk + 1, t, nact, top, top_ring, A.ccodes, boff,
                                               code_ring);
         cp_async_commit();
       }
@@ -253,8 +255,8 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       const int jA = s - t, jB = jA - G;
       const uint2 wa = pa[k], wb = pb[k];
       {
-        const int ca = min(int(code_ring[(boff + jA + 1) & (kCodeRing16 - 1)]), kLetters - 1);
-        const int cb = min(int(code_ring[(boff + jB + 1) & (kCodeRing16 - 1)]), kLetters - 1);
+        const int ca = min(int(code_ring[(boff + jA + 1) & (kCodeRing16 - 1)]), ncls - 1);
+        const int cb = min(int(code_ring[(boff + jB + 1) & (kCodeRing16 - 1)]), ncls - 1);
         pa[k ^ 1] = profA[(2 * ca) * kThreads16];
         pb[k ^ 1] = profB[(2 * cb) * kThreads16];
       }
@@ -413,10 +415,10 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
 template <bool LOCAL, bool CHECK>
 __global__ void __launch_bounds__(kThreads16) fill_i16_kernel(const FillArgs A) {
   extern __shared__ __align__(16) uint8_t smem[];
-  int8_t *s_mat = reinterpret_cast<int8_t *>(smem);
+  int8_t *s_mat = reinterpret_cast<int8_t *>(smem);  // class scores, nclasses x nclasses
   uint2 *s_prof = reinterpret_cast<uint2 *>(smem + kMatBytes);
-  uint8_t *s_rings = smem + kMatBytes + 2 * kLetters * kThreads16 * sizeof(uint2);
-  for (int k = threadIdx.x; k < kLetters * kLetters; k += blockDim.x) s_mat[k] = A.matrix[k];
+  uint8_t *s_rings = smem + kMatBytes + size_t(2 * A.nclasses) * kThreads16 * sizeof(uint2);
+  for (int k = threadIdx.x; k < A.nclasses * A.nclasses; k += blockDim.x) s_mat[k] = A.cmatrix[k];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;

@@ -189,7 +189,7 @@ extern "C" int tsq_align_score_noalloc(const uint8_t *d_seqs, int64_t seqs_len, 
   uint8_t *scratch = ds->scratch;
   na_prepare_kernel<<<1, 256, 0, st>>>(tab, scratch);
   if (cudaGetLastError() != cudaSuccess) return TSQ_E_CUDA;
-  if (launch_encode(d_seqs, seqs_len, scratch + kOffLut, scratch + kOffCodes, st) != cudaSuccess) return TSQ_E_CUDA;
+  if (launch_encode(d_seqs, seqs_len, scratch + kOffLut, scratch + kOffCodes, nullptr, nullptr, st) != cudaSuccess) return TSQ_E_CUDA;
   na_validate_kernel<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<const PairDev *>(d_pairs), n, seqs_len,
                                                        max_len, reinterpret_cast<ResultDev *>(d_out), scratch);
   if (cudaGetLastError() != cudaSuccess) return TSQ_E_CUDA;

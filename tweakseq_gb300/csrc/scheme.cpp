@@ -68,6 +68,26 @@ void finish(Scheme *s) {
       if (s->score[x][y] != s->score[y][x]) s->symmetric = false;
     }
   if (s->max_score < s->min_score) s->max_score = s->min_score = 0;
+  // Score classes, numbered in letter order of their first letter.
+  int rep[kLetters];
+  s->nclasses = 0;
+  for (int x = 0; x < kLetters; ++x) {
+    s->cls[x] = kBadCode;
+    if (!s->valid[x]) continue;
+    for (int c = 0; c < s->nclasses && s->cls[x] == kBadCode; ++c) {
+      const int r = rep[c];
+      bool same = true;
+      for (int y = 0; y < kLetters && same; ++y)
+        if (s->valid[y]) same = s->score[x][y] == s->score[r][y] && s->score[y][x] == s->score[y][r];
+      if (same) s->cls[x] = uint8_t(c);
+    }
+    if (s->cls[x] == kBadCode) {
+      rep[s->nclasses] = x;
+      s->cls[x] = uint8_t(s->nclasses++);
+    }
+  }
+  for (int a = 0; a < s->nclasses; ++a)
+    for (int b = 0; b < s->nclasses; ++b) s->cscore[a * s->nclasses + b] = s->score[rep[a]][rep[b]];
 }
 
 }  // namespace
@@ -107,6 +127,12 @@ void build_lut(const Scheme &s, uint8_t lut[256]) {
   for (int c = 0; c < 256; ++c) lut[c] = kBadCode;
   for (int x = 0; x < kLetters; ++x)
     if (s.valid[x]) lut['A' + x] = uint8_t(x);
+}
+
+void build_class_lut(const Scheme &s, uint8_t lut[256]) {
+  for (int c = 0; c < 256; ++c) lut[c] = kBadCode;
+  for (int x = 0; x < kLetters; ++x)
+    if (s.valid[x]) lut['A' + x] = s.cls[x];
 }
 
 }  // namespace tsq

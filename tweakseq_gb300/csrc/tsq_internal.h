@@ -36,6 +36,12 @@ struct Scheme {
   uint8_t valid[kLetters];
   int32_t max_score, min_score;
   bool symmetric;
+  // Score classes: valid letters with the same row and column of scores
+  // (BLOSUM62: J, O, U and X) share a class; the int16x2 score fill indexes
+  // its profile by class, which keeps the profile small.
+  int32_t nclasses;
+  uint8_t cls[kLetters];               // class of each letter, kBadCode if invalid
+  int8_t cscore[kLetters * kLetters];  // nclasses x nclasses class scores
 };
 
 struct PairDev {
@@ -78,6 +84,9 @@ struct FillArgs {
   int32_t *overflow;     // int16 CHECK: per pair, 1 when a lane came near 32767
   int32_t max_score;     // largest substitution score of the scheme
   uint32_t one;          // int16x2 fill: 1, an opaque multiplier for packed subtractions on the IMAD pipe
+  const uint8_t *ccodes;  // int16x2 fill: class code per residue (kBadCode invalid), same offsets as codes
+  const int8_t *cmatrix;  // int16x2 fill: nclasses x nclasses class scores
+  int32_t nclasses;
 };
 
 // Compacts the pairs an int16 CHECK launch flagged into a warp-task list
@@ -107,13 +116,17 @@ int build_scheme(const tsq_params *p, Scheme *out);
 // BLOSUM62 entry by row index in the order ARNDCQEGHILKMFPSTWYVBZX.
 int8_t blosum62_by_row(int x, int y);
 void build_lut(const Scheme &s, uint8_t lut[256]);
+// Byte -> score class (kBadCode for bytes the scheme rejects).
+void build_class_lut(const Scheme &s, uint8_t lut[256]);
 
 // Kernel launchers (fill_kernels.cu, walk_kernel.cu, encode in batch.cu).
 // Returns the number of thread blocks a persistent launch of this shape uses.
 // A launch covers every lane width G of one row height R and lane type
 // (i16: 0 int32, 1 int16x2, 2 int16x2 with overflow check).
-int fill_blocks(int R, int i16, int out_mode, bool local);
-size_t fill_smem_bytes(int R, int i16, int out_mode);
+// Blocks of a fill launch resident on the device; nclasses sizes the int16x2
+// fill's profile (ignored by the int32 fills).
+int fill_blocks(int R, int i16, int out_mode, bool local, int nclasses = kLetters);
+size_t fill_smem_bytes(int R, int i16, int out_mode, int nclasses = kLetters);
 int fill_threads();
 int fill_threads_for(int i16);
 size_t fill_bnd_entry_bytes(int i16, int out_mode);
@@ -126,8 +139,10 @@ int cta_blocks(int out_mode, bool local);
 size_t cta_bnd_entry_bytes(int out_mode);
 cudaError_t launch_cta(int out_mode, bool local, const FillArgs &a, int blocks, cudaStream_t st);
 cudaError_t launch_walk(const WalkArgs &a, cudaStream_t st);
+// Residues -> letter codes and, when clut_dev / ccodes are set, score
+// classes.
 cudaError_t launch_encode(const uint8_t *seqs, int64_t len, const uint8_t *lut_dev, uint8_t *codes,
-                          cudaStream_t st);
+                          const uint8_t *clut_dev, uint8_t *ccodes, cudaStream_t st);
 
 // Bytes of traceback planes a pair needs under a shape.
 inline int64_t plane_bytes(int m, int n, const Shape &sh) {

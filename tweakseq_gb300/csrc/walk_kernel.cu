@@ -136,30 +136,42 @@ __global__ void walk_kernel(const WalkArgs A) {
   res.n_ident = ident;
 }
 
+// ASCII -> letter codes, and (when clut is set) -> score classes for the
+// int16x2 fill, through shared-memory tables.
 __global__ void encode_kernel(const uint8_t *__restrict__ seqs, int64_t len, const uint8_t *__restrict__ lut,
-                              uint8_t *__restrict__ codes) {
-  __shared__ uint8_t s_lut[256];
+                              uint8_t *__restrict__ codes, const uint8_t *__restrict__ clut,
+                              uint8_t *__restrict__ ccodes) {
+  __shared__ uint8_t s_lut[256], s_clut[256];
   s_lut[threadIdx.x] = lut[threadIdx.x];
+  s_clut[threadIdx.x] = clut ? clut[threadIdx.x] : uint8_t(0);
   __syncthreads();
   // 16 residues per thread per iteration through 128-bit loads where the
   // buffer allows it; the tail goes byte by byte.
   const int64_t nvec = len / 16;
   const uint4 *src = reinterpret_cast<const uint4 *>(seqs);
   uint4 *dst = reinterpret_cast<uint4 *>(codes);
+  uint4 *cdst = reinterpret_cast<uint4 *>(ccodes);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += stride) {
-    uint4 w = src[v];
+    const uint4 w0 = src[v];
+    uint4 w = w0, c = w0;
     uint32_t *x = reinterpret_cast<uint32_t *>(&w);
+    uint32_t *y = reinterpret_cast<uint32_t *>(&c);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const uint32_t u = x[q];
       x[q] = uint32_t(s_lut[u & 0xFF]) | (uint32_t(s_lut[(u >> 8) & 0xFF]) << 8) |
              (uint32_t(s_lut[(u >> 16) & 0xFF]) << 16) | (uint32_t(s_lut[u >> 24]) << 24);
+      y[q] = uint32_t(s_clut[u & 0xFF]) | (uint32_t(s_clut[(u >> 8) & 0xFF]) << 8) |
+             (uint32_t(s_clut[(u >> 16) & 0xFF]) << 16) | (uint32_t(s_clut[u >> 24]) << 24);
     }
     dst[v] = w;
+    if (ccodes) cdst[v] = c;
   }
-  for (int64_t k = nvec * 16 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < len; k += stride)
+  for (int64_t k = nvec * 16 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < len; k += stride) {
     codes[k] = s_lut[seqs[k]];
+    if (ccodes) ccodes[k] = s_clut[seqs[k]];
+  }
 }
 
 }  // namespace
@@ -173,7 +185,7 @@ cudaError_t launch_walk(const WalkArgs &a, cudaStream_t st) {
 }
 
 cudaError_t launch_encode(const uint8_t *seqs, int64_t len, const uint8_t *lut_dev, uint8_t *codes,
-                          cudaStream_t st) {
+                          const uint8_t *clut_dev, uint8_t *ccodes, cudaStream_t st) {
   if (len <= 0) return cudaSuccess;
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
@@ -181,7 +193,7 @@ cudaError_t launch_encode(const uint8_t *seqs, int64_t len, const uint8_t *lut_d
   const int64_t work = (len + 15) / 16;
   int blocks = int(std::min<int64_t>((work + 255) / 256, (int64_t)sms * 8));
   if (blocks < 1) blocks = 1;
-  encode_kernel<<<blocks, 256, 0, st>>>(seqs, len, lut_dev, codes);
+  encode_kernel<<<blocks, 256, 0, st>>>(seqs, len, lut_dev, codes, clut_dev, ccodes);
   return cudaGetLastError();
 }
 
