@@ -10,7 +10,7 @@
 namespace tsq {
 namespace fill {
 
-constexpr int kThreads = 256;   // 8 warps per block
+constexpr int kThreads = 128;   // 4 warps per block
 constexpr int kMatBytes = 704;  // 26*26 int8 rounded up to a 64-byte multiple
 constexpr int kAhead = 4;       // step-loop unroll
 

@@ -430,11 +430,12 @@ __device__ __forceinline__ void fill_warp_task(const FillArgs &A, const int8_t *
   }
 }
 
-// Residency target per SM: 2 blocks (16 warps) for score and traceback
-// fills; identity fills carry path counts and take what they need.
+// Residency target per SM: 4 blocks (16 warps) for score and traceback
+// fills (128 registers); identity fills carry path counts: 3 blocks (12
+// warps, 170 registers).
 template <int OUT>
 struct MinBlocks {
-  static constexpr int value = OUT == kOutIdent ? 1 : 2;
+  static constexpr int value = OUT == kOutIdent ? 3 : 4;
 };
 
 template <int R, bool LOCAL, int OUT>
