@@ -19,6 +19,7 @@
 // kernel always finishes.
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 
 #include "fill_common.cuh"
@@ -227,160 +228,174 @@ __global__ void __launch_bounds__(kCtaThreads, 1) fill_cta_kernel(const FillArgs
       tv[0] = top_at(0);
       const int max_steps = n + G - 1;
 
-      for (int s0 = 0; s0 < max_steps; s0 += 2) {
+      // Steps [G, n_int) have every lane in range (and lane 0's next top
+      // entry inside the row): no range tests there.  Both ends even, so
+      // the double-buffer slot of a step is its parity in every segment.
+      const int i0 = min(G, max_steps & ~1);
+      const int i1 = max(i0, (n - 1) & ~1);
+      auto step = [&](const int s, auto k_tag, auto interior_tag) {
+        constexpr int k = decltype(k_tag)::value;
+        constexpr bool INTERIOR = decltype(interior_tag)::value;
+        if (((s + 1) & (kChunk - 1)) == 0) {
+          // Consumer: the next chunk must be there before lane 0
+          // prefetches its first column; report what was read.
+          cp_async_wait_all();
+          __syncwarp();
+          if (w == 0) {
+            stage_global((s + 1) / kChunk + 1);
+          } else {
+            stage_codes((s + 1) / kChunk + 1, t, n, A.codes, boff, code_ring);
+            if (lane == 0) {
+              __threadfence_block();  // the entries read so far are in registers
+              cons[w] = base + min(s + 2, n);
+            }
+            cta_wait_geq(&prod[w], base + min(s + 1 + kChunk + 1, n), fail);
+          }
+          cp_async_commit();
+        }
+        if ((s & (kChunk - 1)) == kChunk - 1) {
+          // Producer: publish the chunk lane 31 finished, then wait for
+          // room for the one it starts (column s - 31).
+          const int done = min(max(s - (G - 1), 0), n);
+          if (lane == G - 1) {
+            __threadfence_block();
+            if (w == kCtaWarps - 1)
+              prod[0] = base + done;
+            else
+              prod[w + 1] = base + done;
+          }
+          if (out_ring && done < n) cta_wait_geq(&cons[w + 1], base + done + kChunk - kCtaRing, fail);
+        }
+        int32_t upH = __shfl_up_sync(0xffffffffu, outH, 1);
+        int32_t upF = __shfl_up_sync(0xffffffffu, outF, 1);
+        uint32_t upCH = 0, upCF = 0;
+        if constexpr (OUT == kOutIdent) {
+          upCH = __shfl_up_sync(0xffffffffu, outCH, 1);
+          upCF = __shfl_up_sync(0xffffffffu, outCF, 1);
+        }
+        const int jj = s - t;
+        const bool valid = INTERIOR || (unsigned)jj < (unsigned)n;
+        const int bc = cb[k & 1];
+        const uint2 pcur = pw[k & 1];
+        cb[(k + 1) & 1] = min(int(code_ring[(boff + jj + 1) & (kCodeRing - 1)]), kLetters - 1);
+        pw[(k + 1) & 1] = prof[cb[(k + 1) & 1] * kCtaThreads];
+        if (t == 0) {
+          upH = tv[k & 1].x;
+          upF = tv[k & 1].y;
+          if constexpr (OUT == kOutIdent) {
+            upCH = uint32_t(tv[k & 1].z);
+            upCF = uint32_t(tv[k & 1].w);
+          }
+          if (INTERIOR || jj + 1 < n) tv[(k + 1) & 1] = top_at(jj + 1);
+        }
+        if (valid) {
+          int32_t hu = upH, fv = upF, d = hdiag;
+          uint32_t chu = upCH, cfv = upCF, cd = cdiag;
+          hdiag = upH;
+          cdiag = upCH;
+          uint32_t tw = 0;
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
-          const int s = s0 + k;
-          if (s < max_steps) {
-            if (((s + 1) & (kChunk - 1)) == 0) {
-              // Consumer: the next chunk must be there before lane 0
-              // prefetches its first column; report what was read.
-              cp_async_wait_all();
-              __syncwarp();
-              if (w == 0) {
-                stage_global((s + 1) / kChunk + 1);
-              } else {
-                stage_codes((s + 1) / kChunk + 1, t, n, A.codes, boff, code_ring);
-                if (lane == 0) {
-                  __threadfence_block();  // the entries read so far are in registers
-                  cons[w] = base + min(s + 2, n);
+          for (int r = 0; r < R; ++r) {
+            const int32_t sc = sbyte_dyn(r < 4 ? pcur.x : pcur.y, r);
+            const int32_t eo = H[r] - oe, ee = E[r] - ge;
+            const int32_t fo = hu - oe, fe = fv - ge;
+            const int32_t e = max(eo, ee);
+            const int32_t f = max(fo, fe);
+            const int32_t dd = d + sc;
+            int32_t h;
+            if constexpr (OUT == kOutScore) {
+              h = LOCAL ? __vimax3_s32_relu(dd, e, f) : __vimax3_s32(dd, e, f);
+              if constexpr (LOCAL) {
+                if (h > best[r]) {
+                  best[r] = h;
+                  bcol[r] = jj + 1;
                 }
-                cta_wait_geq(&prod[w], base + min(s + 1 + kChunk + 1, n), fail);
               }
-              cp_async_commit();
-            }
-            if ((s & (kChunk - 1)) == kChunk - 1) {
-              // Producer: publish the chunk lane 31 finished, then wait for
-              // room for the one it starts (column s - 31).
-              const int done = min(max(s - (G - 1), 0), n);
-              if (lane == G - 1) {
-                __threadfence_block();
-                if (w == kCtaWarps - 1)
-                  prod[0] = base + done;
-                else
-                  prod[w + 1] = base + done;
+            } else {
+              const bool eopen = eo >= ee, fopen = fo >= fe;
+              int dir = kDirDiag;
+              h = dd;
+              if (e > h) {
+                h = e;
+                dir = kDirE;
               }
-              if (out_ring && done < n) cta_wait_geq(&cons[w + 1], base + done + kChunk - kCtaRing, fail);
-            }
-            int32_t upH = __shfl_up_sync(0xffffffffu, outH, 1);
-            int32_t upF = __shfl_up_sync(0xffffffffu, outF, 1);
-            uint32_t upCH = 0, upCF = 0;
-            if constexpr (OUT == kOutIdent) {
-              upCH = __shfl_up_sync(0xffffffffu, outCH, 1);
-              upCF = __shfl_up_sync(0xffffffffu, outCF, 1);
-            }
-            const int jj = s - t;
-            const bool valid = (unsigned)jj < (unsigned)n;
-            const int bc = cb[k & 1];
-            const uint2 pcur = pw[k & 1];
-            cb[(k + 1) & 1] = min(int(code_ring[(boff + jj + 1) & (kCodeRing - 1)]), kLetters - 1);
-            pw[(k + 1) & 1] = prof[cb[(k + 1) & 1] * kCtaThreads];
-            if (t == 0) {
-              upH = tv[k & 1].x;
-              upF = tv[k & 1].y;
+              if (f > h) {
+                h = f;
+                dir = kDirF;
+              }
+              if (LOCAL && h <= 0) {
+                h = 0;
+                dir = kDirStop;
+              }
               if constexpr (OUT == kOutIdent) {
-                upCH = uint32_t(tv[k & 1].z);
-                upCF = uint32_t(tv[k & 1].w);
-              }
-              if (jj + 1 < n) tv[(k + 1) & 1] = top_at(jj + 1);
-            }
-            if (valid) {
-              int32_t hu = upH, fv = upF, d = hdiag;
-              uint32_t chu = upCH, cfv = upCF, cd = cdiag;
-              hdiag = upH;
-              cdiag = upCH;
-              uint32_t tw = 0;
-#pragma unroll
-              for (int r = 0; r < R; ++r) {
-                const int32_t sc = sbyte_dyn(r < 4 ? pcur.x : pcur.y, r);
-                const int32_t eo = H[r] - oe, ee = E[r] - ge;
-                const int32_t fo = hu - oe, fe = fv - ge;
-                const int32_t e = max(eo, ee);
-                const int32_t f = max(fo, fe);
-                const int32_t dd = d + sc;
-                int32_t h;
-                if constexpr (OUT == kOutScore) {
-                  h = LOCAL ? __vimax3_s32_relu(dd, e, f) : __vimax3_s32(dd, e, f);
-                  if constexpr (LOCAL) {
-                    if (h > best[r]) {
-                      best[r] = h;
-                      bcol[r] = jj + 1;
-                    }
-                  }
-                } else {
-                  const bool eopen = eo >= ee, fopen = fo >= fe;
-                  int dir = kDirDiag;
-                  h = dd;
-                  if (e > h) {
-                    h = e;
-                    dir = kDirE;
-                  }
-                  if (f > h) {
-                    h = f;
-                    dir = kDirF;
-                  }
-                  if (LOCAL && h <= 0) {
-                    h = 0;
-                    dir = kDirStop;
-                  }
-                  if constexpr (OUT == kOutIdent) {
-                    const uint32_t ce = (eopen ? cH[r] : cE[r]) + kCol;
-                    const uint32_t cfn = (fopen ? chu : cfv) + kCol;
-                    const uint32_t cdd = cd + (qa[r] == bc ? kIdentCol : kCol);
-                    uint32_t ch = dir == kDirDiag ? cdd : (dir == kDirE ? ce : cfn);
-                    if (LOCAL && dir == kDirStop) ch = 0u;
-                    cd = cH[r];
-                    cH[r] = ch;
-                    cE[r] = ce;
-                    chu = ch;
-                    cfv = cfn;
-                    if constexpr (LOCAL) {
-                      if (h > best[r]) {
-                        best[r] = h;
-                        bcol[r] = jj + 1;
-                        bcnt[r] = ch;
-                      }
-                    }
-                  } else {
-                    tw |= uint32_t(dir | (eopen ? 4 : 0) | (fopen ? 8 : 0)) << (4 * r);
-                    if constexpr (LOCAL) {
-                      if (h > best[r]) {
-                        best[r] = h;
-                        bcol[r] = jj + 1;
-                      }
-                    }
+                const uint32_t ce = (eopen ? cH[r] : cE[r]) + kCol;
+                const uint32_t cfn = (fopen ? chu : cfv) + kCol;
+                const uint32_t cdd = cd + (qa[r] == bc ? kIdentCol : kCol);
+                uint32_t ch = dir == kDirDiag ? cdd : (dir == kDirE ? ce : cfn);
+                if (LOCAL && dir == kDirStop) ch = 0u;
+                cd = cH[r];
+                cH[r] = ch;
+                cE[r] = ce;
+                chu = ch;
+                cfv = cfn;
+                if constexpr (LOCAL) {
+                  if (h > best[r]) {
+                    best[r] = h;
+                    bcol[r] = jj + 1;
+                    bcnt[r] = ch;
                   }
                 }
-                d = H[r];
-                H[r] = h;
-                E[r] = e;
-                hu = h;
-                fv = f;
-              }
-              outH = hu;
-              outF = fv;
-              outCH = chu;
-              outCF = cfv;
-              if (t == G - 1) {
-                Top v;
-                v.x = outH;
-                v.y = outF;
-                if constexpr (OUT == kOutIdent) {
-                  v.z = int32_t(outCH);
-                  v.w = int32_t(outCF);
+              } else {
+                tw |= uint32_t(dir | (eopen ? 4 : 0) | (fopen ? 8 : 0)) << (4 * r);
+                if constexpr (LOCAL) {
+                  if (h > best[r]) {
+                    best[r] = h;
+                    bcol[r] = jj + 1;
+                  }
                 }
-                if (w == kCtaWarps - 1)
-                  grow[jj] = v;
-                else if (out_ring)
-                  out_ring[(base + jj) % kCtaRing] = v;
-              }
-              if constexpr (OUT == kOutTrace) {
-                const int64_t entry = ((int64_t)band * (n + G - 1) + s) * G + t;
-                reinterpret_cast<uint32_t *>(planes)[entry] = tw;
               }
             }
+            d = H[r];
+            H[r] = h;
+            E[r] = e;
+            hu = h;
+            fv = f;
+          }
+          outH = hu;
+          outF = fv;
+          outCH = chu;
+          outCF = cfv;
+          if (t == G - 1) {
+            Top v;
+            v.x = outH;
+            v.y = outF;
+            if constexpr (OUT == kOutIdent) {
+              v.z = int32_t(outCH);
+              v.w = int32_t(outCF);
+            }
+            if (w == kCtaWarps - 1)
+              grow[jj] = v;
+            else if (out_ring)
+              out_ring[(base + jj) % kCtaRing] = v;
+          }
+          if constexpr (OUT == kOutTrace) {
+            const int64_t entry = ((int64_t)band * (n + G - 1) + s) * G + t;
+            reinterpret_cast<uint32_t *>(planes)[entry] = tw;
           }
         }
+      };
+      int s0 = 0;
+      for (; s0 < i0; s0 += 2) {
+        step(s0, IntTag<0>{}, BoolTag<false>{});
+        if (s0 + 1 < max_steps) step(s0 + 1, IntTag<1>{}, BoolTag<false>{});
+      }
+      for (; s0 < i1; s0 += 2) {
+        step(s0, IntTag<0>{}, BoolTag<true>{});
+        step(s0 + 1, IntTag<1>{}, BoolTag<true>{});
+      }
+      for (; s0 < max_steps; s0 += 2) {
+        step(s0, IntTag<0>{}, BoolTag<false>{});
+        if (s0 + 1 < max_steps) step(s0 + 1, IntTag<1>{}, BoolTag<false>{});
       }
       cp_async_wait_all();
       __syncwarp();
