@@ -62,6 +62,8 @@ def parse_args():
     ap.add_argument("--no-configs", action="store_true", help="skip the other configurations")
     ap.add_argument("--configs-only", action="store_true", help="run only the other configurations")
     ap.add_argument("--msa-only", action="store_true", help="run only the consensus and guide-tree legs")
+    ap.add_argument("--profile-case", choices=["long_dna", "identity", "consensus"], default=None,
+                    help="small profiling case of another kernel (for ncu)")
     return ap.parse_args()
 
 
@@ -580,6 +582,61 @@ def msa_leg(cpu_cols=40, cpu_tree_leaves=1000):
     return out
 
 
+def run_profile_case(args):
+    """Small cases for ncu of the kernels behind the other measurements:
+    long_dna (32 DNA pairs of 10-12 kb with traceback: the CTA fill and the
+    walker),
+    identity (200,000 pairs of the guide-tree all-vs-all: the int32 identity
+    fill), consensus (100,000 x 2,000 alignment: the class-count kernel).
+    Device-resident, no graph, warm-up then timed runs."""
+    import torch
+
+    from tweakseq_gb300 import _native as N
+    from tweakseq_gb300 import aligner as A
+    from tweakseq_gb300 import build as B
+    from tweakseq_gb300 import workloads as W
+
+    B.build()
+    case = args.profile_case
+    if case in ("long_dna", "identity"):
+        if case == "long_dna":
+            ps = W.long_dna_pairs(32, lo=10_000, hi=12_000)
+            kw = dict(matrix="dna", gap_open=5, gap_extend=2, output="alignment")
+        else:
+            ps = W.guide_tree_families()
+            ps = ps.subset(np.arange(200_000))
+            kw = dict(output="identity")
+        with A.Batch(ps, use_graph=False, **kw) as b:
+            for _ in range(args.warmup + args.steps):
+                b.run()
+            st = b.stats()
+        print(json.dumps({"profile_case": case, "pairs": len(ps), "cells": ps.cells, "fill_ms": st["fill_ms"],
+                          "device_ms": st["device_ms"], "fill_gcups": ps.cells / (st["fill_ms"] * 1e-3) / 1e9}))
+        return
+    if case == "consensus":
+        nseq, ncols = 100_000, 2000
+        rng = np.random.default_rng(nseq)
+        fav = W.random_protein(rng, ncols)
+        rows = W.AA_LETTERS[rng.integers(0, 20, size=(nseq, ncols), dtype=np.uint8)]
+        u = rng.integers(0, 100, size=(nseq, ncols), dtype=np.uint8)
+        rows = np.ascontiguousarray(np.where(u < 60, fav[None, :], rows), dtype=np.uint8)
+        rows[u >= 85] = ord("-")
+        L = N.lib()
+        d_rows = torch.from_numpy(rows).cuda()
+        d_out = torch.zeros(ncols, dtype=torch.uint8, device="cuda")
+        nb = L.tsq_consensus_scratch_bytes(ncols)
+        scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+        st = torch.cuda.current_stream()
+        for _ in range(args.warmup + args.steps):
+            rc = L.tsq_consensus_device(d_rows.data_ptr(), nseq, ncols, ncols, -1.0, d_out.data_ptr(), None, None,
+                                        scratch.data_ptr(), nb, st.cuda_stream)
+            assert rc == 0
+        st.synchronize()
+        print(json.dumps({"profile_case": case, "rows": nseq, "cols": ncols, "bytes": nseq * ncols}))
+        return
+    raise SystemExit(f"unknown profile case {case}")
+
+
 def run_profile(args):
     """Small case for ncu: the device-resident batch over a prefix of the
     workload, launched without a graph so each kernel is a separate launch."""
@@ -605,6 +662,9 @@ def main():
     args = parse_args()
     if args.profile:
         run_profile(args)
+        return
+    if args.profile_case:
+        run_profile_case(args)
         return
     if args.configs_only:
         from tweakseq_gb300 import build as B
