@@ -241,10 +241,11 @@ __device__ __forceinline__ void fill_warp_task(const FillArgs &A, const int8_t *
 #pragma unroll
           for (int r = 0; r < R; ++r) {
             const int32_t sc = sbyte_dyn(r < 4 ? pcur.x : pcur.y, r);
-            const int32_t eo = H[r] - oe, ee = E[r] - ge;
-            const int32_t fo = hu - oe, fe = fv - ge;
-            const int32_t e = max(eo, ee);
-            const int32_t f = max(fo, fe);
+            // E and F: opening beats extending on ties (one DPX max with its
+            // predicate each).
+            bool eopen, fopen;
+            const int32_t e = __vibmax_s32(H[r] - oe, E[r] - ge, &eopen);
+            const int32_t f = __vibmax_s32(hu - oe, fv - ge, &fopen);
             const int32_t dd = d + sc;
             int32_t h;
             if constexpr (OUT == kOutScore) {
@@ -256,17 +257,12 @@ __device__ __forceinline__ void fill_warp_task(const FillArgs &A, const int8_t *
                 }
               }
             } else {
-              const bool eopen = eo >= ee, fopen = fo >= fe;
-              int dir = kDirDiag;
-              h = dd;
-              if (e > h) {
-                h = e;
-                dir = kDirE;
-              }
-              if (f > h) {
-                h = f;
-                dir = kDirF;
-              }
+              // H: diagonal beats E beats F on ties: pde = (diag >= E),
+              // pxf = (max(diag, E) >= F).
+              bool pde, pxf;
+              const int32_t x = __vibmax_s32(dd, e, &pde);
+              h = __vibmax_s32(x, f, &pxf);
+              int dir = pxf ? (pde ? int(kDirDiag) : int(kDirE)) : int(kDirF);
               if (LOCAL && h <= 0) {
                 h = 0;
                 dir = kDirStop;
@@ -275,8 +271,8 @@ __device__ __forceinline__ void fill_warp_task(const FillArgs &A, const int8_t *
                 const uint32_t ce = (eopen ? cH[r] : cE[r]) + kCol;
                 const uint32_t cfn = (fopen ? chu : cfv) + kCol;
                 const uint32_t cdd = cd + (qa[r] == bc ? kIdentCol : kCol);
-                uint32_t ch = dir == kDirDiag ? cdd : (dir == kDirE ? ce : cfn);
-                if (LOCAL && dir == kDirStop) ch = 0u;
+                uint32_t ch = pxf ? (pde ? cdd : ce) : cfn;
+                if (LOCAL && h <= 0) ch = 0u;
                 cd = cH[r];
                 cH[r] = ch;
                 cE[r] = ce;
