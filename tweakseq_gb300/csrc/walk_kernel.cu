@@ -15,25 +15,84 @@
 namespace tsq {
 namespace {
 
-struct PlaneReader {
-  const uint8_t *base;
-  int n, G, R;
-  __device__ int nib(int i, int j) const {
-    // (i, j) are 1-based cell coordinates with i, j >= 1.
-    const int P = G * R;
+constexpr int kWalkThreads = 128;
+constexpr int kWin = 16;  // steps per plane window
+
+// Direction nibbles of one pair, read through a window: the words of steps
+// ws-15..ws for lanes wt-1 and wt of one band, loaded together into this
+// thread's shared-memory slots.  A walk moves one step left or one row up
+// at a time, so most nibbles come from the window and the window's 32 loads
+// are independent of each other (one global-memory latency per refill
+// instead of one per step).  Row i is tracked as (band, lane t, row r).
+struct PlaneWalk {
+  const uint32_t *words;  // planes as 32-bit entries: 8 rows x 4 bits
+  uint32_t *win;          // 2 * kWin shared words of this thread
+  int n, G, P;
+  int band, t, r;                       // position of row i (1-based i >= 1)
+  int wband = -1, wt = -1, ws = -1;     // the window
+  __device__ void set_row(int i) {
     const int row0 = i - 1;
-    const int pass = row0 / P;
-    const int w = row0 - pass * P;
-    const int t = w / R;
-    const int r = w - t * R;
-    const int s = (j - 1) + t;
-    const int64_t entry = ((int64_t)pass * (n + G - 1) + s) * G + t;
-    const int64_t byte = entry * (R / 2) + (r >> 1);
-    return (base[byte] >> ((r & 1) * 4)) & 15;
+    band = row0 / P;
+    const int w = row0 - band * P;
+    t = w >> 3;
+    r = w & 7;
+  }
+  __device__ void up() {  // i -> i - 1
+    if (--r < 0) {
+      r = 7;
+      if (--t < 0) {
+        t = G - 1;
+        --band;
+      }
+    }
+  }
+  __device__ void refill(int s) {
+    wband = band;
+    wt = t;
+    ws = s;
+    const int64_t row = (int64_t)band * (n + G - 1);
+    // All loads first (addresses clamped into the band, unused slots read a
+    // valid word), then the stores: the loads overlap instead of each
+    // waiting for the previous store.
+    uint32_t v[2 * kWin];
+#pragma unroll
+    for (int k = 0; k < kWin; ++k) {
+      const int64_t e = (row + max(s - k, 0)) * G + t;
+      v[2 * k + 1] = __ldg(words + e);
+      v[2 * k] = __ldg(words + (t > 0 ? e - 1 : e));
+    }
+#pragma unroll
+    for (int k = 0; k < 2 * kWin; ++k) win[k] = v[k];
+  }
+  // Nibble of cell (i, j), i the current row, j >= 1.
+  __device__ int nib(int j) {
+    const int s = j - 1 + t;
+    if (band != wband || (t != wt && t != wt - 1) || s > ws || s <= ws - kWin) refill(s);
+    const uint32_t w = win[2 * (ws - s) + (t == wt ? 1 : 0)];
+    return int(w >> (4 * r)) & 15;
   }
 };
 
-__global__ void walk_kernel(const WalkArgs A) {
+// One sequence read backwards through a 16-byte window.
+struct SeqWalk {
+  const uint8_t *base;
+  uintptr_t blk = ~uintptr_t(0);
+  uint4 v;
+  __device__ uint8_t at(int idx) {
+    const uintptr_t addr = reinterpret_cast<uintptr_t>(base) + uintptr_t(idx);
+    const uintptr_t b = addr & ~uintptr_t(15);
+    if (b != blk) {
+      v = *reinterpret_cast<const uint4 *>(b);
+      blk = b;
+    }
+    const int o = int(addr - b);
+    const uint32_t w = o < 8 ? (o < 4 ? v.x : v.y) : (o < 12 ? v.z : v.w);
+    return uint8_t(w >> (8 * (o & 3)));
+  }
+};
+
+__global__ void __launch_bounds__(kWalkThreads) walk_kernel(const WalkArgs A) {
+  __shared__ uint32_t s_win[kWalkThreads * 2 * kWin];
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= A.n_tasks) return;
   const int p = A.tasks[k];
@@ -41,12 +100,13 @@ __global__ void walk_kernel(const WalkArgs A) {
   ResultDev &res = A.res[p];
   if (res.status != TSQ_OK) return;
   const int m = pr.a_len, n = pr.b_len;
-  const uint8_t *a = A.seqs + pr.a_off;
-  const uint8_t *b = A.seqs + pr.b_off;
+  SeqWalk a{A.seqs + pr.a_off}, b{A.seqs + pr.b_off};
   const int64_t cap = (int64_t)m + n;
   char *out_a = A.aln + A.aln_off[p];
   char *out_b = out_a + cap;
-  PlaneReader pl{A.planes + A.plane_off[p], n, A.shape_G[p], A.shape_R[p]};
+  const int G = A.shape_G[p];
+  PlaneWalk pl{reinterpret_cast<const uint32_t *>(A.planes + A.plane_off[p]), s_win + threadIdx.x * 2 * kWin, n, G,
+               G * A.shape_R[p]};
 
   int i, j;
   if (A.local) {
@@ -61,6 +121,7 @@ __global__ void walk_kernel(const WalkArgs A) {
     i = m;
     j = n;
   }
+  if (i > 0) pl.set_row(i);
   int state = 0;  // 0 = H, 1 = E, 2 = F
   int64_t L = 0;
   int ident = 0;
@@ -71,32 +132,35 @@ __global__ void walk_kernel(const WalkArgs A) {
     }
     if (state == 0) {
       if (A.local) {
-        if (i == 0 || j == 0 || (pl.nib(i, j) & 3) == kDirStop) break;
+        if (i == 0 || j == 0 || (pl.nib(j) & 3) == kDirStop) break;
       } else if (i == 0 && j == 0) {
         break;
       }
       if (i == 0) {  // global top row: one horizontal gap run
         ++L;
         out_a[cap - L] = '-';
-        out_b[cap - L] = char(b[j - 1]);
+        out_b[cap - L] = char(b.at(j - 1));
         --j;
         continue;
       }
       if (j == 0) {  // global left column: one vertical gap run
         ++L;
-        out_a[cap - L] = char(a[i - 1]);
+        out_a[cap - L] = char(a.at(i - 1));
         out_b[cap - L] = '-';
         --i;
+        if (i > 0) pl.up();
         continue;
       }
-      const int hd = pl.nib(i, j) & 3;
+      const int hd = pl.nib(j) & 3;
       if (hd == kDirDiag) {
         ++L;
-        out_a[cap - L] = char(a[i - 1]);
-        out_b[cap - L] = char(b[j - 1]);
-        ident += a[i - 1] == b[j - 1];
+        const uint8_t ca = a.at(i - 1), cb = b.at(j - 1);
+        out_a[cap - L] = char(ca);
+        out_b[cap - L] = char(cb);
+        ident += ca == cb;
         --i;
         --j;
+        if (i > 0) pl.up();
       } else {
         state = hd;
       }
@@ -107,10 +171,10 @@ __global__ void walk_kernel(const WalkArgs A) {
         res.status = TSQ_E_CUDA;
         return;
       }
-      const int d = pl.nib(i, j);
+      const int d = pl.nib(j);
       ++L;
       out_a[cap - L] = '-';
-      out_b[cap - L] = char(b[j - 1]);
+      out_b[cap - L] = char(b.at(j - 1));
       --j;
       if (d & 4) state = 0;
     } else {
@@ -118,11 +182,12 @@ __global__ void walk_kernel(const WalkArgs A) {
         res.status = TSQ_E_CUDA;
         return;
       }
-      const int d = pl.nib(i, j);
+      const int d = pl.nib(j);
       ++L;
-      out_a[cap - L] = char(a[i - 1]);
+      out_a[cap - L] = char(a.at(i - 1));
       out_b[cap - L] = '-';
       --i;
+      if (i > 0) pl.up();
       if (d & 8) state = 0;
     }
   }
@@ -178,9 +243,8 @@ __global__ void encode_kernel(const uint8_t *__restrict__ seqs, int64_t len, con
 
 cudaError_t launch_walk(const WalkArgs &a, cudaStream_t st) {
   if (a.n_tasks <= 0) return cudaSuccess;
-  const int threads = 128;
-  const int blocks = (a.n_tasks + threads - 1) / threads;
-  walk_kernel<<<blocks, threads, 0, st>>>(a);
+  const int blocks = (a.n_tasks + kWalkThreads - 1) / kWalkThreads;
+  walk_kernel<<<blocks, kWalkThreads, 0, st>>>(a);
   return cudaGetLastError();
 }
 
