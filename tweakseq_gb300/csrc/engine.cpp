@@ -254,29 +254,43 @@ namespace tsq {
 namespace {
 int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t seqs_len,
               const tsq_pair_desc *pairs, int64_t n, const tsq_params *p, const tsq_batch_opts *opts, bool plain,
-              int64_t call_pairs, int64_t call_cells);
+              int64_t call_pairs, int64_t call_cells, bool segmented);
 }  // namespace
 
 int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *pairs, int64_t n,
                const tsq_params *p, const tsq_batch_opts *opts, bool plain) {
-  return plan_impl(b, nullptr, seqs, seqs_len, pairs, n, p, opts, plain, 0, 0);
+  return plan_impl(b, nullptr, seqs, seqs_len, pairs, n, p, opts, plain, 0, 0, false);
 }
 
 int batch_plan_chunk(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t seqs_len,
                      const tsq_pair_desc *pairs, int64_t n, const tsq_params *p, const tsq_batch_opts *opts,
-                     int64_t call_pairs, int64_t call_cells) {
+                     int64_t call_pairs, int64_t call_cells, bool segmented) {
   if (!b || owner == b || call_pairs < n || call_cells < 0) return TSQ_E_INVALID_ARG;
-  if (!owner) return plan_impl(b, nullptr, seqs, seqs_len, pairs, n, p, opts, false, call_pairs, call_cells);
+  if (!owner)
+    return plan_impl(b, nullptr, seqs, seqs_len, pairs, n, p, opts, false, call_pairs, call_cells, segmented);
   const tsq_batch_opts o{owner->device, 0, opts ? opts->autotune : 0, 0};
-  return plan_impl(b, owner, nullptr, owner->seqs_len, pairs, n, p, &o, false, call_pairs, call_cells);
+  return plan_impl(b, owner, nullptr, owner->seqs_len, pairs, n, p, &o, false, call_pairs, call_cells, segmented);
+}
+
+int input_segment(const tsq_batch *owner, const uint8_t *seqs, int64_t begin, int64_t end, cudaStream_t stream) {
+  if (!owner || begin < 0 || end > owner->seqs_len || begin % 16 != 0 || (end > begin && !seqs))
+    return TSQ_E_INVALID_ARG;
+  if (end <= begin) return TSQ_OK;
+  TSQ_TRY(cudaMemcpyAsync(owner->seqs.as<uint8_t>() + begin, seqs + begin, size_t(end - begin),
+                          cudaMemcpyHostToDevice, stream));
+  TSQ_TRY(launch_encode(owner->seqs.as<uint8_t>() + begin, end - begin, owner->lut.as<uint8_t>(),
+                        owner->codes.as<uint8_t>() + begin, owner->classes ? owner->clut.as<uint8_t>() : nullptr,
+                        owner->classes ? owner->ccodes.as<uint8_t>() + begin : nullptr, stream));
+  return TSQ_OK;
 }
 
 namespace {
 int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t seqs_len,
               const tsq_pair_desc *pairs, int64_t n, const tsq_params *p, const tsq_batch_opts *opts, bool plain,
-              int64_t call_pairs, int64_t call_cells) {
+              int64_t call_pairs, int64_t call_cells, bool segmented) {
   if (!b || !p || n < 0 || seqs_len < 0) return TSQ_E_INVALID_ARG;
   b->input_owner = owner;
+  b->input_segmented = segmented;
   if (n > 0 && !pairs) return TSQ_E_INVALID_ARG;
   if (seqs_len > 0 && !seqs && !owner) return TSQ_E_INVALID_ARG;
   if (n > INT32_MAX / 2) return TSQ_E_TOO_LARGE;
@@ -401,7 +415,8 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
     TSQ_TRY(b->seqs.ensure(size_t(seqs_len) + 128));
     TSQ_TRY(b->codes.ensure(size_t(seqs_len) + 128));
     if (b->classes) TSQ_TRY(b->ccodes.ensure(size_t(seqs_len) + 128));
-    if (seqs_len > 0) TSQ_TRY(cudaMemcpyAsync(b->seqs.p, seqs, size_t(seqs_len), cudaMemcpyHostToDevice, b->stream));
+    if (seqs_len > 0 && !segmented)
+      TSQ_TRY(cudaMemcpyAsync(b->seqs.p, seqs, size_t(seqs_len), cudaMemcpyHostToDevice, b->stream));
   }
 
   // ---- lane types, shapes and order (one parallel pass over the pairs) ----
@@ -761,7 +776,11 @@ int enqueue_run(tsq_batch *b) {
   const int nl = int(b->launches.size());
   TSQ_TRY(cudaMemsetAsync(b->counters.p, 0, sizeof(int32_t) * (size_t(nl) + 2), st));
   TSQ_TRY(record(b, 0));
-  if (b->input_owner) {
+  if (b->input_segmented) {
+    // The residues this chunk reads were uploaded and encoded on the call's
+    // input stream.
+    TSQ_TRY(cudaStreamWaitEvent(st, b->input_ready, 0));
+  } else if (b->input_owner) {
     // The owner encodes the residues on its stream.
     TSQ_TRY(cudaStreamWaitEvent(st, b->input_owner->ev_encoded, 0));
   } else {

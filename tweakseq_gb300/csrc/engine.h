@@ -123,6 +123,11 @@ struct tsq_batch {
   // this object's fills wait on that object's ev_encoded.
   const tsq_batch *input_owner = nullptr;
   cudaEvent_t ev_encoded = nullptr;  // recorded after this object's encode
+  // Segmented input (chunks of one call): the residues arrive in segments
+  // uploaded and encoded on the caller's input stream (input_segment); the
+  // fills wait on input_ready, the event after this chunk's segment.
+  bool input_segmented = false;
+  cudaEvent_t input_ready = nullptr;
 
   tsq::DevBuf seqs, codes, pairs, tasks, wtasks, res, bnd, planes, plane_off, aln, aln_off, shape_g, shape_r, counters,
       lut, matrix, overflow, rerun_tasks, rerun_wtasks;
@@ -150,7 +155,11 @@ int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pa
 // call would give it.
 int batch_plan_chunk(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t seqs_len,
                      const tsq_pair_desc *pairs, int64_t n, const tsq_params *p, const tsq_batch_opts *opts,
-                     int64_t call_pairs, int64_t call_cells);
+                     int64_t call_pairs, int64_t call_cells, bool segmented);
+// Uploads residues [begin, end) of `seqs` into the owner's device buffers and
+// encodes them, on `stream`; begin is a multiple of 16.  The owner must be
+// planned (its code tables are on the device).
+int input_segment(const tsq_batch *owner, const uint8_t *seqs, int64_t begin, int64_t end, cudaStream_t stream);
 int batch_run_async(tsq_batch *b);
 int batch_sync(tsq_batch *b);
 int batch_results(tsq_batch *b, tsq_result *out);
