@@ -148,11 +148,33 @@ int align_in_waves(tsq_batch *e, const uint8_t *seqs, int64_t seqs_len, const ts
   std::vector<tsq_pair_desc> wave;
   std::vector<tsq_result> res;
   int status = TSQ_OK;
+  // Long pairs run one per CTA (the CTA fill): a wave that holds more of them
+  // than one round of resident CTAs is cut at a whole number of rounds, or
+  // its last few long pairs would start only when the first ones finish.
+  const int slots = tsq::cta_blocks(tsq::kOutTrace, p->mode == TSQ_LOCAL);
+  auto is_long = [&](int64_t k) {
+    const tsq_pair_desc &d = pairs[k];
+    return d.a_len > 0 && d.b_len > 0 && double((d.a_len + 255) / 256) * double(d.b_len + 31) > 20000.0;
+  };
   int64_t begin = 0;
   while (begin < n) {
     int64_t end = begin, used = 0;
     while (end < n && (end == begin || used + bytes[size_t(order[size_t(end)])] <= budget))
       used += bytes[size_t(order[size_t(end++)])];
+    if (slots > 0 && used <= budget) {
+      int64_t nlong = 0;
+      for (int64_t k = begin; k < end; ++k) nlong += is_long(order[size_t(k)]);
+      if (nlong > slots && nlong % slots != 0) {
+        const int64_t keep = nlong / slots * slots;
+        int64_t seen = 0, cut = end;
+        for (int64_t k = begin; k < end; ++k)
+          if (is_long(order[size_t(k)]) && seen++ == keep) {
+            cut = k;
+            break;
+          }
+        end = cut;
+      }
+    }
     if (used > budget) {  // one pair alone is larger than the budget
       for (int64_t k = begin; k < end; ++k) out[order[size_t(k)]].status = TSQ_E_TOO_LARGE;
       status = status ? status : TSQ_E_TOO_LARGE;
@@ -246,12 +268,14 @@ int tsq_align_batch(const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *
       // planes do not fit in the device memory that is free runs in waves:
       // pairs by plane size, largest first (so that the pairs of a wave are
       // alike and no wave waits on one long pair), each wave as many pairs as
-      // fit in 60 % of the free memory.  Results land at the pairs' own
+      // fit in 85 % of the free memory less 2 GiB (the rest of the batch
+      // object: residues, rows, results, strings).  Results land at the pairs' own
       // positions; a pair too large for any wave is TSQ_E_TOO_LARGE.
       if (cudaSetDevice(dev) != cudaSuccess) return TSQ_E_CUDA;
       size_t free_b = 0, total_b = 0;
       if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return TSQ_E_CUDA;
-      int64_t budget = int64_t(0.6 * double(free_b + e->planes.cap + e->aln.cap));
+      const double avail = double(free_b + e->planes.cap + e->aln.cap);
+      int64_t budget = std::max(int64_t(0.85 * avail) - (int64_t(2) << 30), int64_t(0.5 * avail));
       // TSQ_WAVE_BUDGET_BYTES lowers the budget (tests use it to force waves).
       if (const char *env = std::getenv("TSQ_WAVE_BUDGET_BYTES")) {
         const long long v = std::atoll(env);
