@@ -18,12 +18,13 @@
 // position of its children), so ties break exactly as in the position-
 // ordered definition: smallest criterion, then smallest position pair.
 //
-// One launch per join.  Every block scans a share of the triangle (rows
-// folded in pairs a, m-2-a so each share has m entries) and writes its best
-// candidate; the last block to finish (atomic ticket, no waiting) reduces
-// the candidates and performs the join: O(m) updates of row/column i, the
-// NJ row sums, the slot move.  The host issues the n-1 launches with the
-// grid sized for the active count m = n - t, which it knows.
+// Two launches per join.  The scan: every block scans a share of the
+// triangle (rows folded in pairs a, m-2-a so each share has m entries) and
+// writes its best candidate; the last block to finish (atomic ticket, no
+// waiting) picks and records the join.  The join: one thread per remaining
+// slot updates the joined cluster's distances, the NJ row sums and the move
+// of the last slot into the freed one.  The host issues the 2(n-1) launches
+// with grids sized for the active count m = n - t, which it knows.
 #include <climits>
 #include <cstring>
 
@@ -38,6 +39,12 @@ struct TreeState {
   int32_t m, t;
   uint32_t ticket;
   int32_t error;
+  // The join the scan picked, for the join launch: slots i and j (pos[i] is
+  // the smaller canonical position lo), the slot a the joined cluster takes
+  // (i unless i is the last slot), the slot f that frees up, and the last
+  // slot L that moves into f.
+  int32_t i, j, a, f, L, lo, si, sj;
+  int64_t dij;
 };
 
 struct Cand {
@@ -114,14 +121,15 @@ struct TreeArgs {
   int32_t n;
 };
 
+// Scan and pick: every block scans its share of the active triangle; the
+// last block to finish (atomic ticket, no waiting) picks the join, records
+// it and leaves the slots to the join launch.
 template <bool NJ>
-__global__ void __launch_bounds__(kTreeThreads) tree_step_kernel(TreeArgs A) {
+__global__ void __launch_bounds__(kTreeThreads) tree_scan_kernel(TreeArgs A, int32_t m, int32_t t) {
   __shared__ Cand sm_c[kTreeThreads / 32];
-  __shared__ int64_t sm_s[kTreeThreads / 32];
   __shared__ bool last;
   const int32_t n = A.n;
-  const int32_t m = A.st->m;
-  if (m < 2) return;
+  if (m < 2 || A.st->error) return;
   const int64_t m2 = m - 2;
 
   Cand best{LLONG_MAX, INT_MAX, INT_MAX, -1, -1};
@@ -154,7 +162,6 @@ __global__ void __launch_bounds__(kTreeThreads) tree_step_kernel(TreeArgs A) {
   if (!last) return;
   __threadfence();
 
-  // The last block: reduce the candidates, then join.
   best = Cand{LLONG_MAX, INT_MAX, INT_MAX, -1, -1};
   for (int k = threadIdx.x; k < int(gridDim.x); k += kTreeThreads) {
     const volatile Cand *vp = A.partial + k;
@@ -162,76 +169,103 @@ __global__ void __launch_bounds__(kTreeThreads) tree_step_kernel(TreeArgs A) {
     if (better(x, best)) best = x;
   }
   best = block_best(best, sm_c);
+  if (threadIdx.x != 0) return;
+  A.st->ticket = 0u;
   if (best.sa < 0) {
-    if (threadIdx.x == 0) A.st->error = 1;
+    A.st->error = 1;  // stops the remaining launches
     return;
   }
   const int32_t i = A.pos[best.sa] == best.lo ? best.sa : best.sb;
   const int32_t j = i == best.sa ? best.sb : best.sa;
   const int64_t dij = A.D[int64_t(i) * n + j];
-  const int32_t t = A.st->t;
   const int32_t si = A.size[i], sj = A.size[j];
-  if (threadIdx.x == 0) {
-    tsq_tree_node o;
-    o.left = A.node[i];
-    o.right = A.node[j];
-    o.size = si + sj;
-    o.pos = best.lo;
-    o.dist = dij;
-    if (NJ) {
-      o.height = 0;
-      o.left_length = m > 2 ? floor_div(m2 * dij + A.r[i] - A.r[j], 2 * m2) : (dij >> 1);
-      o.right_length = dij - o.left_length;
-    } else {
-      const int64_t h = dij >> 1;
-      o.height = h;
-      o.left_length = h - A.height[i];
-      o.right_length = h - A.height[j];
-    }
-    A.out[t] = o;
+  tsq_tree_node o;
+  o.left = A.node[i];
+  o.right = A.node[j];
+  o.size = si + sj;
+  o.pos = best.lo;
+  o.dist = dij;
+  if (NJ) {
+    o.height = 0;
+    o.left_length = m > 2 ? floor_div(m2 * dij + A.r[i] - A.r[j], 2 * m2) : (dij >> 1);
+    o.right_length = dij - o.left_length;
+  } else {
+    const int64_t h = dij >> 1;
+    o.height = h;
+    o.left_length = h - A.height[i];
+    o.right_length = h - A.height[j];
   }
-  __syncthreads();  // row sums and heights read above before they change below
+  A.out[t] = o;
+  const int32_t L = m - 1;
+  const int32_t a = i != L ? i : j;
+  A.st->i = i;
+  A.st->j = j;
+  A.st->a = a;
+  A.st->f = a == i ? j : i;
+  A.st->L = L;
+  A.st->lo = best.lo;
+  A.st->si = si;
+  A.st->sj = sj;
+  A.st->dij = dij;
+  A.st->m = m - 1;  // for the host's final check only: the launches take m and t as arguments
+  A.st->t = t + 1;
+  if (NJ) A.r[a] = 0;  // the join launch adds the new row sum into it
+}
 
+// The join: one thread per remaining slot k.  Thread k writes the joined
+// cluster's distance to k (row and column a) and, when the last slot L moves
+// into the freed slot f, L's distance to k (row and column f); slot L's own
+// thread writes the distance between the joined cluster and L at (a, f).
+// Every thread touches only its own k's entries of rows/columns a and f and
+// reads only rows i, j and L, so the updates are independent.
+template <bool NJ>
+__global__ void __launch_bounds__(kTreeThreads) tree_join_kernel(TreeArgs A, int32_t m, int32_t t) {
+  __shared__ int64_t sm_s[kTreeThreads / 32];
+  const TreeState st = *A.st;
+  const int32_t n = A.n;
+  if (m < 2 || st.error) return;
+  const int32_t i = st.i, j = st.j, a = st.a, f = st.f, L = st.L;
+  const int64_t dij = st.dij, si = st.si, sj = st.sj;
+  const bool move = f != L;
   int64_t rsum = 0;
-  for (int32_t k = threadIdx.x; k < m; k += kTreeThreads) {
+  for (int32_t k = blockIdx.x * kTreeThreads + threadIdx.x; k < m; k += gridDim.x * kTreeThreads) {
     if (k == i || k == j) continue;
     const int64_t dik = A.D[int64_t(i) * n + k], djk = A.D[int64_t(j) * n + k];
-    const int64_t du = NJ ? (dik + djk - dij) >> 1 : floor_div(si * dik + sj * djk, int64_t(si) + sj);
-    if (NJ) A.r[k] += du - dik - djk;
+    const int64_t du = NJ ? (dik + djk - dij) >> 1 : floor_div(si * dik + sj * djk, si + sj);
     rsum += du;
-    A.D[int64_t(i) * n + k] = du;
-    A.D[int64_t(k) * n + i] = du;
-  }
-  rsum = block_sum(rsum, sm_s);
-  if (threadIdx.x == 0) {
-    if (NJ) A.r[i] = rsum;
-    if (!NJ) A.height[i] = dij >> 1;
-    A.node[i] = n + t;
-    A.size[i] = si + sj;
-  }
-  __syncthreads();
-
-  // Slot j leaves: the last slot moves into it.
-  const int32_t L = m - 1;
-  if (j != L) {
-    for (int32_t k = threadIdx.x; k < L; k += kTreeThreads) {
-      A.D[int64_t(j) * n + k] = A.D[int64_t(L) * n + k];
-      A.D[int64_t(k) * n + j] = A.D[int64_t(k) * n + L];
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      A.D[int64_t(j) * n + j] = 0;
-      A.r[j] = A.r[L];
-      A.height[j] = A.height[L];
-      A.pos[j] = A.pos[L];
-      A.node[j] = A.node[L];
-      A.size[j] = A.size[L];
+    const int64_t rk = NJ ? A.r[k] + du - dik - djk : 0;
+    if (move && k == L) {
+      // L takes slot f.
+      A.D[int64_t(a) * n + f] = du;
+      A.D[int64_t(f) * n + a] = du;
+      A.D[int64_t(f) * n + f] = 0;
+      if (NJ) A.r[f] = rk;
+      A.height[f] = A.height[L];
+      A.pos[f] = A.pos[L];
+      A.node[f] = A.node[L];
+      A.size[f] = A.size[L];
+    } else {
+      A.D[int64_t(a) * n + k] = du;
+      A.D[int64_t(k) * n + a] = du;
+      if (NJ) A.r[k] = rk;
+      if (move) {
+        const int64_t dlk = A.D[int64_t(L) * n + k];
+        A.D[int64_t(f) * n + k] = dlk;
+        A.D[int64_t(k) * n + f] = dlk;
+      }
     }
   }
-  if (threadIdx.x == 0) {
-    A.st->m = m - 1;
-    A.st->t = t + 1;
-    A.st->ticket = 0u;
+  if (NJ) {
+    rsum = block_sum(rsum, sm_s);
+    if (threadIdx.x == 0 && rsum != 0) atomicAdd(reinterpret_cast<unsigned long long *>(A.r + a),
+                                                 static_cast<unsigned long long>(rsum));
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (!NJ) A.height[a] = dij >> 1;
+    A.node[a] = n + t;
+    A.size[a] = int32_t(si + sj);
+    A.pos[a] = st.lo;
+    A.D[int64_t(a) * n + a] = 0;
   }
 }
 
@@ -333,10 +367,14 @@ int tree_run(const TreeArgs &A, int32_t method, cudaStream_t s, tsq_tree_node *o
   for (int32_t t = 0; t < n - 1; ++t) {
     const int32_t m = n - t;
     const int blocks = std::max(1, std::min(parts, m / 2));
-    if (method == TSQ_TREE_NJ)
-      tree_step_kernel<true><<<blocks, kTreeThreads, 0, s>>>(A);
-    else
-      tree_step_kernel<false><<<blocks, kTreeThreads, 0, s>>>(A);
+    const int jblocks = std::max(1, std::min(parts, (m + kTreeThreads - 1) / kTreeThreads));
+    if (method == TSQ_TREE_NJ) {
+      tree_scan_kernel<true><<<blocks, kTreeThreads, 0, s>>>(A, m, t);
+      tree_join_kernel<true><<<jblocks, kTreeThreads, 0, s>>>(A, m, t);
+    } else {
+      tree_scan_kernel<false><<<blocks, kTreeThreads, 0, s>>>(A, m, t);
+      tree_join_kernel<false><<<jblocks, kTreeThreads, 0, s>>>(A, m, t);
+    }
   }
   cudaError_t e = cudaGetLastError();
   TreeState st{};
