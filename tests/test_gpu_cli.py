@@ -67,3 +67,52 @@ def test_all_vs_all_identity_table(tmp_path):
             assert rows[k][:5] == [f"p{x}", f"p{y}", str(want.score), str(want.n_ident), str(want.n_cols)]
             k += 1
     assert k == len(rows)
+
+
+def _parse_newick(text):
+    """Leaf-set splits and leaf order of a Newick string (no quoting)."""
+    import re
+    order = re.findall(r"[(,]([A-Za-z0-9_]+):", text)
+    return order
+
+
+def test_guide_tree_newick(tmp_path):
+    from tweakseq_gb300 import msa
+
+    rng = np.random.default_rng(4)
+    recs = []
+    for k in range(12):
+        s = W.random_protein(rng, int(rng.integers(80, 200))).tobytes().decode()
+        recs.append(F.Record(f">s{k}", f"s{k}", s))
+    fin, fout = tmp_path / "in.fa", tmp_path / "tree.dnd"
+    F.write(str(fin), recs)
+    for method in ("upgma", "nj"):
+        r = subprocess.run([B.CLI, "-i", str(fin), "-o", str(fout), "--tree", method], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        text = fout.read_text().strip()
+        # The same tree as the library's from the oracle's identities.
+        ps = W._pairset_from_lists([x.sequence.encode() for x in recs],
+                                   np.stack(np.triu_indices(12, 1), 1))
+        want = O.batch(ps.seqs, ps.a_off, ps.a_len, ps.b_off, ps.b_len, mode=O.MODE_IDENT)
+        joins = O.guide_tree(O.identity_distances(12, want["n_ident"], want["n_cols"]), N_TREE[method])
+        tree = msa.Tree(12, joins, method)
+        assert text == tree.newick([x.label for x in recs])
+        assert sorted(_parse_newick(text)) == sorted(x.label for x in recs)
+
+
+N_TREE = {"upgma": 0, "nj": 1}
+
+
+def test_consensus_line(tmp_path):
+    rows = ["AAA-IWW", "A-AaVWW", "A-A.IW-"]
+    recs = [F.Record(f">r{k}", f"r{k}", r) for k, r in enumerate(rows)]
+    fin, fout = tmp_path / "aln.fa", tmp_path / "cons.fa"
+    F.write(str(fin), recs)
+    r = subprocess.run([B.CLI, "-i", str(fin), "-o", str(fout), "--consensus"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = F.read(str(fout))
+    assert out[0].label == "consensus" and out[0].sequence == "A?A-IW?"
+    # Rows of different lengths are refused.
+    F.write(str(fin), recs + [F.Record(">short", "short", "AAA")])
+    r = subprocess.run([B.CLI, "-i", str(fin), "-o", str(fout), "--consensus"], capture_output=True, text=True)
+    assert r.returncode == 1 and "equal length" in r.stderr

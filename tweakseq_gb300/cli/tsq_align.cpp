@@ -14,13 +14,21 @@
 //                     own FASTA writer wraps at 80, FASTAFile.cpp:149-171);
 //   --all-vs-all   -> every unordered pair, one TSV line per pair: labels,
 //                     score, identical columns, columns, percent identity
-//                     (the distance input of a guide tree).
+//                     (the distance input of a guide tree);
+//   --tree upgma|nj -> the guide tree of the sequences from their all-vs-all
+//                     identities, as Newick text (branch lengths in
+//                     distance units, distance = 1 - identity);
+//   --consensus    -> the input is an alignment (equal-length gapped rows,
+//                     kept as they are); one FASTA record with the consensus
+//                     line the editor draws (Consensus::calculate,
+//                     tweakseq/Core/Annotations/Consensus.cpp:80-161).
 //
 // FASTA is read as the editor reads it (FASTAFile.cpp:71-147): a record
 // starts at '>' or ';', its label is the header text up to the first space,
 // further ';' lines right after a header are comments, sequence lines are
 // concatenated.  Gap characters already in the input ('-', '.') are dropped
-// and residues upper-cased, as the external aligners do with editor output.
+// and residues upper-cased, as the external aligners do with editor output
+// (except for --consensus, which reads the rows verbatim).
 #include <cctype>
 #include <cstdio>
 #include <cstdlib>
@@ -41,7 +49,7 @@ struct Record {
   std::string residues;
 };
 
-bool read_fasta(std::istream &in, std::vector<Record> &out, std::string &err) {
+bool read_fasta(std::istream &in, std::vector<Record> &out, std::string &err, bool verbatim) {
   std::string line;
   enum { kSeek, kComment, kSequence } state = kSeek;
   while (std::getline(in, line)) {
@@ -64,7 +72,12 @@ bool read_fasta(std::istream &in, std::vector<Record> &out, std::string &err) {
     }
     if (state == kSeek) continue;
     for (char ch : line) {
-      if (ch == '-' || ch == '.' || std::isspace(static_cast<unsigned char>(ch))) continue;
+      if (std::isspace(static_cast<unsigned char>(ch))) continue;
+      if (verbatim) {
+        out.back().residues.push_back(ch);
+        continue;
+      }
+      if (ch == '-' || ch == '.') continue;
       out.back().residues.push_back(char(std::toupper(static_cast<unsigned char>(ch))));
     }
     state = kSequence;
@@ -84,9 +97,26 @@ void write_wrapped(std::ostream &o, const std::string &header, const std::string
 void usage() {
   std::fprintf(stderr,
                "usage: tsq_align [-in|-i FILE] [-out|-o FILE] [--local] [--dna | --matrix blosum62|dna]\n"
-               "                 [--gap-open N] [--gap-extend N] [--all-vs-all]\n"
+               "                 [--gap-open N] [--gap-extend N] [--all-vs-all | --tree upgma|nj | --consensus]\n"
                "  Two sequences: gapped FASTA of their alignment (stdout when no output file).\n"
-               "  --all-vs-all: TSV of every pair (label_a, label_b, score, n_ident, n_cols, identity %%).\n");
+               "  --all-vs-all: TSV of every pair (label_a, label_b, score, n_ident, n_cols, identity %%).\n"
+               "  --tree: Newick guide tree from all-vs-all identities (UPGMA or neighbour joining).\n"
+               "  --consensus: consensus line of an alignment (equal-length rows) as one FASTA record.\n");
+}
+
+// Newick text of the joins (leaves 0..n-1, join t is node n + t).
+std::string newick(const std::vector<tsq_tree_node> &nodes, const std::vector<Record> &recs) {
+  const int n = int(recs.size());
+  std::vector<std::string> text(size_t(2 * n - 1));
+  for (int k = 0; k < n; ++k) text[size_t(k)] = recs[size_t(k)].label;
+  for (int t = 0; t < n - 1; ++t) {
+    const tsq_tree_node &nd = nodes[size_t(t)];
+    char la[64], lb[64];
+    std::snprintf(la, sizeof(la), ":%.6f", double(nd.left_length) / 4294967296.0);
+    std::snprintf(lb, sizeof(lb), ":%.6f", double(nd.right_length) / 4294967296.0);
+    text[size_t(n + t)] = "(" + text[size_t(nd.left)] + la + "," + text[size_t(nd.right)] + lb + ")";
+  }
+  return (n == 1 ? text[0] : text[size_t(2 * n - 2)]) + ";";
 }
 
 const char *status_name(int rc) {
@@ -111,7 +141,8 @@ int main(int argc, char **argv) {
   p.mode = TSQ_GLOBAL;
   p.output = TSQ_OUT_ALIGNMENT;
   p.lane = TSQ_LANE_AUTO;
-  bool all_vs_all = false, gaps_set = false;
+  bool all_vs_all = false, gaps_set = false, consensus = false;
+  int tree = -1;
   for (int k = 1; k < argc; ++k) {
     const std::string a = argv[k];
     auto next = [&](const char *what) -> std::string {
@@ -140,6 +171,16 @@ int main(int argc, char **argv) {
       p.gap_extend = std::atoi(next("--gap-extend").c_str());
       gaps_set = true;
     } else if (a == "--all-vs-all") all_vs_all = true;
+    else if (a == "--consensus") consensus = true;
+    else if (a == "--tree") {
+      const std::string m = next("--tree");
+      if (m == "upgma") tree = TSQ_TREE_UPGMA;
+      else if (m == "nj") tree = TSQ_TREE_NJ;
+      else {
+        std::fprintf(stderr, "tsq_align: unknown tree method %s\n", m.c_str());
+        return 2;
+      }
+    }
     else if (a == "-h" || a == "--help") {
       usage();
       return 0;
@@ -167,7 +208,7 @@ int main(int argc, char **argv) {
       }
       in = &f;
     }
-    if (!read_fasta(*in, recs, err)) {
+    if (!read_fasta(*in, recs, err, consensus)) {
       std::fprintf(stderr, "tsq_align: %s\n", err.c_str());
       return 1;
     }
@@ -183,7 +224,30 @@ int main(int argc, char **argv) {
     out = &fo;
   }
 
-  if (!all_vs_all) {
+  if (consensus) {
+    const size_t cols = recs[0].residues.size();
+    std::string rows;
+    for (const Record &r : recs) {
+      if (r.residues.size() != cols) {
+        std::fprintf(stderr, "tsq_align: --consensus needs rows of equal length (%s has %zu, not %zu)\n",
+                     r.label.c_str(), r.residues.size(), cols);
+        return 1;
+      }
+      rows += r.residues;
+    }
+    std::string cons(cols, '?');
+    const int rc = tsq_consensus(reinterpret_cast<const uint8_t *>(rows.data()), int32_t(recs.size()),
+                                 int32_t(cols), int64_t(cols), -1.0, reinterpret_cast<uint8_t *>(&cons[0]), nullptr,
+                                 nullptr);
+    if (rc != TSQ_OK) {
+      std::fprintf(stderr, "tsq_align: %s\n", status_name(rc));
+      return 1;
+    }
+    write_wrapped(*out, ">consensus", cons);
+    return 0;
+  }
+
+  if (!all_vs_all && tree < 0) {
     if (recs.size() != 2) {
       std::fprintf(stderr, "tsq_align: pairwise alignment needs exactly 2 sequences (got %zu); "
                            "use --all-vs-all for more\n",
@@ -224,6 +288,22 @@ int main(int argc, char **argv) {
   if (rc != TSQ_OK) {
     std::fprintf(stderr, "tsq_align: %s\n", status_name(rc));
     return 1;
+  }
+  if (tree >= 0) {
+    std::vector<int32_t> ident(res.size()), ncols(res.size());
+    for (size_t k = 0; k < res.size(); ++k) {
+      ident[k] = res[k].n_ident;
+      ncols[k] = res[k].n_cols;
+    }
+    std::vector<tsq_tree_node> nodes(recs.size() > 1 ? recs.size() - 1 : 1);
+    const int trc = tsq_guide_tree(int32_t(recs.size()), ident.data(), ncols.data(), tree, nodes.data());
+    if (trc != TSQ_OK) {
+      std::fprintf(stderr, "tsq_align: %s\n", status_name(trc));
+      return 1;
+    }
+    nodes.resize(recs.size() - 1);
+    *out << newick(nodes, recs) << '\n';
+    return 0;
   }
   *out << "label_a\tlabel_b\tscore\tn_ident\tn_cols\tidentity_pct\n";
   size_t k = 0;
