@@ -9,12 +9,12 @@
 // the plurality (default nseq / 2, :163-172), else '?'.
 //
 // A row's sum depends only on its class (23 BLOSUM62 rows + the gap class),
-// so the kernel counts classes per column and first row per class (one pass
-// over the bytes, HBM-bound), and the finishing kernel evaluates the 24
-// class sums from the counts: score(x) = sum_y count(y) S(x,y) - S(x,x).
-// All terms are integers, so this equals the reference's double sums
-// exactly; the first row with the best score is the smallest first-row index
-// among the best classes.
+// so the kernel counts classes per column (one pass over the bytes,
+// HBM-bound), and the finishing kernel evaluates the 24 class sums from the
+// counts: score(x) = sum_y count(y) S(x,y) - S(x,x), then scans the column
+// from the first row for the first row whose class holds the best sum.  All
+// terms are integers, so this equals the reference's double sums exactly,
+// and the row found is the first row with the best score, as there.
 #include <climits>
 #include <cstring>
 
@@ -35,23 +35,18 @@ __constant__ uint8_t c_class[256];                // byte -> class
 // A block covers 128 columns (lane t holds columns t, t+32, t+64, t+96 of
 // the tile, so that its counters fall in bank t) and one slice of the rows,
 // striped over its 8 warps.  With 4-byte-aligned rows a lane reads its 4
-// columns of a row with one 32-bit load.  Counts and first rows go to one
-// shared histogram per block (shared-memory atomics; the first-row minimum
-// is only attempted when the row can lower it), then into the column totals
-// with global atomics.
+// columns of a row with one 32-bit load, eight rows' loads in flight.  The
+// counts go to one shared histogram per block (shared-memory atomics), then
+// into the column totals with global atomics.  Only counts: the first row of
+// a class is needed for the winning classes alone and is found afterwards.
 template <bool kVec>
 __global__ void __launch_bounds__(kCountThreads) consensus_count_kernel(const uint8_t *__restrict__ rows, int32_t nseq,
                                                                         int32_t ncols, int64_t stride,
-                                                                        int32_t rows_per_slice, uint32_t *cnt,
-                                                                        int32_t *first) {
+                                                                        int32_t rows_per_slice, uint32_t *cnt) {
   __shared__ uint32_t h[kClasses][kTile];
-  __shared__ int32_t f[kClasses][kTile];
   __shared__ uint8_t cls[256];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int k = threadIdx.x; k < kClasses * kTile; k += kCountThreads) {
-    (&h[0][0])[k] = 0u;
-    (&f[0][0])[k] = INT_MAX;
-  }
+  for (int k = threadIdx.x; k < kClasses * kTile; k += kCountThreads) (&h[0][0])[k] = 0u;
   for (int k = threadIdx.x; k < 256; k += kCountThreads) cls[k] = c_class[k];
   __syncthreads();
   const int32_t c0 = blockIdx.x * kTile;
@@ -68,27 +63,21 @@ __global__ void __launch_bounds__(kCountThreads) consensus_count_kernel(const ui
       for (int u = 0; u < nvalid; ++u) v |= uint32_t(__ldg(p + int64_t(r) * stride + u)) << (8 * u);
       return v;
     };
-    auto count = [&](int32_t r, uint32_t v) {
+    auto count = [&](uint32_t v) {
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        if (u < nvalid) {
-          const int c = cls[(v >> (8 * u)) & 0xffu];
-          const int slot = lane + 32 * u;
-          atomicAdd(&h[c][slot], 1u);
-          if (r < f[c][slot]) atomicMin(&f[c][slot], r);
-        }
-      }
+      for (int u = 0; u < 4; ++u)
+        if (u < nvalid) atomicAdd(&h[cls[(v >> (8 * u)) & 0xffu]][lane + 32 * u], 1u);
     };
+    constexpr int kRows = 8;
     int32_t r = r0 + w;
-    // Four rows' loads in flight before their counts.
-    for (; r + 3 * kCountWarps < r1; r += 4 * kCountWarps) {
-      uint32_t v[4];
+    for (; r + (kRows - 1) * kCountWarps < r1; r += kRows * kCountWarps) {
+      uint32_t v[kRows];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) v[q] = load(r + q * kCountWarps);
+      for (int q = 0; q < kRows; ++q) v[q] = load(r + q * kCountWarps);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) count(r + q * kCountWarps, v[q]);
+      for (int q = 0; q < kRows; ++q) count(v[q]);
     }
-    for (; r < r1; r += kCountWarps) count(r, load(r));
+    for (; r < r1; r += kCountWarps) count(load(r));
   }
   __syncthreads();
   for (int e = threadIdx.x; e < kClasses * kTile; e += kCountThreads) {
@@ -96,55 +85,69 @@ __global__ void __launch_bounds__(kCountThreads) consensus_count_kernel(const ui
     const uint32_t s = h[c][slot];
     // Tile slot lane + 32u holds memory column c0 + 4*lane + u.
     const int32_t col = c0 + 4 * (slot & 31) + (slot >> 5);
-    if (s != 0u && col < ncols) {
-      atomicAdd(&cnt[int64_t(col) * kClasses + c], s);
-      atomicMin(&first[int64_t(col) * kClasses + c], f[c][slot]);
-    }
+    if (s != 0u && col < ncols) atomicAdd(&cnt[int64_t(col) * kClasses + c], s);
   }
 }
 
-__global__ void consensus_init_kernel(uint32_t *cnt, int32_t *first, int64_t n) {
-  for (int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; k < n; k += int64_t(gridDim.x) * blockDim.x) {
+__global__ void consensus_init_kernel(uint32_t *cnt, int64_t n) {
+  for (int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; k < n; k += int64_t(gridDim.x) * blockDim.x)
     cnt[k] = 0u;
-    first[k] = INT_MAX;
-  }
 }
 
-// One thread per column: the 24 class sums from the counts.
-__global__ void consensus_finish_kernel(const uint8_t *__restrict__ rows, int32_t ncols, int64_t stride,
-                                        double plurality, const uint32_t *__restrict__ cnt,
-                                        const int32_t *__restrict__ first, uint8_t *out, int32_t *best_score,
-                                        int32_t *best_matches) {
+// One thread per column: the 24 class sums from the counts, then the first
+// row (in row order) whose class has the highest sum -- the row the
+// reference's loop settles on.  The scan usually ends within a few rows (a
+// winning class is a frequent one); consecutive threads read consecutive
+// columns of a row.
+__global__ void consensus_finish_kernel(const uint8_t *__restrict__ rows, int32_t nseq, int32_t ncols, int64_t stride,
+                                        double plurality, const uint32_t *__restrict__ cnt, uint8_t *out,
+                                        int32_t *best_score, int32_t *best_matches) {
+  __shared__ uint8_t cls[256];
+  for (int k = threadIdx.x; k < 256; k += blockDim.x) cls[k] = c_class[k];
+  __syncthreads();
   const int32_t col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncols) return;
   int64_t n[kClasses];
 #pragma unroll
   for (int y = 0; y < kClasses; ++y) n[y] = cnt[int64_t(col) * kClasses + y];
-  int64_t bs = 0, bm = 0;
-  int32_t bf = INT_MAX;
-  bool have = false;
+  int64_t bs = 0;
+  uint32_t winners = 0u;  // classes holding the best sum
+  int64_t score[kClasses], match[kClasses];
 #pragma unroll
   for (int x = 0; x < kClasses; ++x) {
-    if (n[x] == 0) continue;
-    int64_t s = 0, mt = 0;
+    int64_t sx = 0, mt = 0;
 #pragma unroll
     for (int y = 0; y < kClasses; ++y) {
       const int v = c_pair[x][y];
-      s += n[y] * v;
+      sx += n[y] * v;
       if (v > 0) mt += n[y];
     }
     // A row does not score against itself.
-    s -= c_pair[x][x];
+    sx -= c_pair[x][x];
     if (c_pair[x][x] > 0) mt -= 1;
-    const int32_t fx = first[int64_t(col) * kClasses + x];
-    if (!have || s > bs || (s == bs && fx < bf)) {
-      have = true;
-      bs = s;
-      bm = mt;
-      bf = fx;
+    score[x] = sx;
+    match[x] = mt;
+    if (n[x] == 0) continue;
+    if (winners == 0u || sx > bs) {
+      bs = sx;
+      winners = 1u << x;
+    } else if (sx == bs) {
+      winners |= 1u << x;
     }
   }
-  out[col] = double(bm) >= plurality ? rows[int64_t(bf) * stride + col] : uint8_t('?');
+  int32_t r = 0;
+  int c = 0;
+  for (; r < nseq; ++r) {
+    c = cls[rows[int64_t(r) * stride + col]];
+    if ((winners >> c) & 1u) break;
+  }
+  if (r >= nseq) r = nseq - 1;  // a winning class always occurs; stays in bounds regardless
+  int64_t bm = 0;
+#pragma unroll
+  for (int x = 0; x < kClasses; ++x)
+    if (x == c) bm = match[x];
+  (void)score;
+  out[col] = double(bm) >= plurality ? rows[int64_t(r) * stride + col] : uint8_t('?');
   if (best_score) best_score[col] = int32_t(bs);
   if (best_matches) best_matches[col] = int32_t(bm);
 }
@@ -202,27 +205,25 @@ cudaError_t consensus_enqueue(const uint8_t *d_rows, int32_t nseq, int32_t ncols
   cudaError_t e = upload_tables();
   if (e != cudaSuccess) return e;
   uint32_t *cnt = static_cast<uint32_t *>(scratch);
-  int32_t *first = reinterpret_cast<int32_t *>(cnt + int64_t(ncols) * kClasses);
   const int64_t entries = int64_t(ncols) * kClasses;
-  consensus_init_kernel<<<int(std::min<int64_t>((entries + 255) / 256, 4096)), 256, 0, stream>>>(cnt, first,
-                                                                                                 entries);
+  consensus_init_kernel<<<int(std::min<int64_t>((entries + 255) / 256, 4096)), 256, 0, stream>>>(cnt, entries);
   // Enough blocks for every SM several times over: split the rows into
   // slices when the columns alone do not give them.
   const int32_t col_tiles = (ncols + kTile - 1) / kTile;
   const int64_t want = int64_t(sm_count()) * 8;
   int32_t slices = int32_t(std::max<int64_t>(1, std::min<int64_t>((want + col_tiles - 1) / col_tiles, 65535)));
   int32_t per = (nseq + slices - 1) / slices;
-  per = std::max(per, 4 * kCountWarps);
+  per = std::max(per, 8 * kCountWarps);
   slices = (nseq + per - 1) / per;
   const bool vec = stride % 4 == 0 && reinterpret_cast<uintptr_t>(d_rows) % 4 == 0;
   if (vec)
     consensus_count_kernel<true><<<dim3(col_tiles, slices), kCountThreads, 0, stream>>>(d_rows, nseq, ncols, stride,
-                                                                                      per, cnt, first);
+                                                                                      per, cnt);
   else
     consensus_count_kernel<false><<<dim3(col_tiles, slices), kCountThreads, 0, stream>>>(d_rows, nseq, ncols, stride,
-                                                                                       per, cnt, first);
-  consensus_finish_kernel<<<(ncols + 127) / 128, 128, 0, stream>>>(d_rows, ncols, stride, plurality, cnt, first,
-                                                                   d_out, d_score, d_matches);
+                                                                                       per, cnt);
+  consensus_finish_kernel<<<(ncols + 127) / 128, 128, 0, stream>>>(d_rows, nseq, ncols, stride, plurality, cnt, d_out,
+                                                                   d_score, d_matches);
   return cudaGetLastError();
 }
 
@@ -237,7 +238,7 @@ struct ConsensusCache {
 
 }  // namespace
 
-size_t consensus_scratch_bytes(int32_t ncols) { return size_t(ncols > 0 ? ncols : 0) * kClasses * 8; }
+size_t consensus_scratch_bytes(int32_t ncols) { return size_t(ncols > 0 ? ncols : 0) * kClasses * 4; }
 
 }  // namespace tsq
 
