@@ -415,17 +415,17 @@ def serve_leg(n_requests=120, loads=(0.25, 0.5, 0.9), seed=5, plain_pairs=600):
 
 
 def configs_leg(c3_pairs=16):
-    """The other configurations (not the headline): C1 all-vs-all 64
-    proteins with traceback (batched vs plain), C3 1,000 long DNA pairs with
-    traceback end to end, and C4 in full (7,998,000 pairs, score +
-    identity).  Each is checked against the oracle."""
+    """The other workloads (not the headline): the all-vs-all of 64 proteins
+    with traceback (batched vs plain), 1,000 long DNA pairs with traceback
+    end to end, and the 4,000-sequence guide-tree all-vs-all (7,998,000
+    pairs, score + identity).  Each is checked against the oracle."""
     from oracle import oracle as O
     from tweakseq_gb300 import aligner as A
     from tweakseq_gb300 import workloads as W
 
     out = {}
     cores = O.num_cores()
-    # C1
+    # All-vs-all of 64 proteins, alignment output.
     ps = W.all_vs_all_proteins()
     with A.Batch(ps, output="alignment", use_graph=True) as b:
         for _ in range(3):
@@ -451,7 +451,7 @@ def configs_leg(c3_pairs=16):
         "pairs": len(ps), "cells": ps.cells, "output": "alignment (global, BLOSUM62 11/1)",
         "batched_gcups": ps.cells / (float(np.median(ms)) * 1e-3) / 1e9, "e2e_gcups": ps.cells / e2e_s / 1e9,
         "plain_gcups": ps.cells / plain_s / 1e9, "mismatches_vs_oracle": mism}
-    # C3: all 1,000 long DNA pairs with traceback through tsq_align_batch,
+    # All 1,000 long DNA pairs with traceback through tsq_align_batch,
     # which runs them in waves sized to the free HBM (their planes need about
     # 500 GB), checked against the oracle on a seeded sample of pairs.
     ps = W.long_dna_pairs(1000)
@@ -470,7 +470,7 @@ def configs_leg(c3_pairs=16):
         "mismatches_vs_oracle": mism + (0 if ok_len else 1),
         "checked": f"{c3_pairs} seeded pairs: score, n_ident, n_cols and string lengths"}
     del res
-    # C4 full
+    # The guide-tree all-vs-all in full.
     ps = W.guide_tree_families()
     with A.Batch(ps, output="identity", use_graph=True) as b:
         b.run()
