@@ -360,10 +360,12 @@ def serve_leg(n_requests=120, loads=(0.25, 0.5, 0.9), seed=5, plain_pairs=600):
 
     cells = np.array([r.pairs.cells for r in reqs], dtype=np.float64)
     total = float(cells.sum())
-    # Warm the server path (planning, first launches) before measuring.
+    # Warm the server path before measuring: one closed-loop pass of the
+    # same requests (first launches, the page-locked result blocks and the
+    # device memory pool a long-running server already holds).
     with A.Server(slots=4) as srv:
-        for r in reqs[:4]:
-            srv.poll(srv.submit(r.pairs, **kw(r)))
+        for rid in [srv.submit(r.pairs, **kw(r)) for r in reqs]:
+            srv.poll(rid)
     with A.Server(slots=4) as srv:
         t0 = time.perf_counter()
         ids = [srv.submit(r.pairs, **kw(r)) for r in reqs]

@@ -21,31 +21,80 @@
 
 namespace tsq {
 
-cudaError_t DevBuf::ensure(size_t bytes) {
+cudaError_t DevBuf::ensure(size_t bytes, cudaStream_t stream) {
   if (bytes == 0) bytes = 16;
   if (bytes <= cap) return cudaSuccess;
-  release();
   const size_t want = (bytes + 255) & ~size_t(255);
-  cudaError_t e = cudaMalloc(&p, want);
+  release();
+  // Stream-ordered allocation takes no device-wide synchronisation, so a
+  // batch object that grows does not wait for kernels other streams run.
+  cudaError_t e = stream ? cudaMallocAsync(&p, want, stream) : cudaMalloc(&p, want);
   if (e != cudaSuccess) {
     p = nullptr;
     return e;
   }
   cap = want;
+  owner = stream;
   return cudaSuccess;
 }
 
 void DevBuf::release() {
-  if (p) cudaFree(p);
+  if (p) {
+    if (owner)
+      cudaFreeAsync(p, owner);
+    else
+      cudaFree(p);
+  }
   p = nullptr;
   cap = 0;
+  owner = nullptr;
 }
+
+// Page-locked host blocks are pooled for the life of the process and not
+// freed: allocating and freeing page-locked memory takes milliseconds per
+// hundred megabytes and can wait for the device, which would stall batches
+// that other threads or server slots have in flight.  Blocks come in
+// power-of-two sizes from 64 KiB; a request takes the smallest idle block of
+// its size class up to four times larger.  The pool keeps at most
+// kPinPoolBytes of idle blocks and frees beyond that (rare: only after a
+// burst of very large batches).
+namespace {
+constexpr size_t kPinMin = size_t(1) << 16;
+constexpr size_t kPinPoolBytes = size_t(8) << 30;
+std::mutex g_pin_mu;
+// (size, block); never destroyed, so buffers released during process exit
+// still find it.
+std::vector<std::pair<size_t, void *>> &g_pin_idle = *new std::vector<std::pair<size_t, void *>>();
+size_t g_pin_idle_bytes = 0;
+
+size_t pin_class(size_t bytes) {
+  size_t c = kPinMin;
+  while (c < bytes) c <<= 1;
+  return c;
+}
+}  // namespace
 
 cudaError_t PinBuf::ensure(size_t bytes) {
   if (bytes == 0) bytes = 16;
   if (bytes <= cap) return cudaSuccess;
   release();
-  const size_t want = (bytes + 4095) & ~size_t(4095);
+  const size_t want = pin_class(bytes);
+  {
+    std::lock_guard<std::mutex> g(g_pin_mu);
+    size_t best = g_pin_idle.size();
+    for (size_t k = 0; k < g_pin_idle.size(); ++k) {
+      const size_t c = g_pin_idle[k].first;
+      if (c >= want && c <= 4 * want && (best == g_pin_idle.size() || c < g_pin_idle[best].first)) best = k;
+    }
+    if (best < g_pin_idle.size()) {
+      p = g_pin_idle[best].second;
+      cap = g_pin_idle[best].first;
+      g_pin_idle[best] = g_pin_idle.back();
+      g_pin_idle.pop_back();
+      g_pin_idle_bytes -= cap;
+      return cudaSuccess;
+    }
+  }
   cudaError_t e = cudaMallocHost(&p, want);
   if (e != cudaSuccess) {
     p = nullptr;
@@ -56,7 +105,18 @@ cudaError_t PinBuf::ensure(size_t bytes) {
 }
 
 void PinBuf::release() {
-  if (p) cudaFreeHost(p);
+  if (p) {
+    bool keep = false;
+    {
+      std::lock_guard<std::mutex> g(g_pin_mu);
+      if (g_pin_idle_bytes + cap <= kPinPoolBytes) {
+        g_pin_idle.emplace_back(cap, p);
+        g_pin_idle_bytes += cap;
+        keep = true;
+      }
+    }
+    if (!keep) cudaFreeHost(p);
+  }
   p = nullptr;
   cap = 0;
 }
@@ -236,7 +296,15 @@ Shape ShapeChooser::pick(int m, int n, int rows_per_lane) const {
 
 }  // namespace tsq
 
+void tsq_batch::release_device_buffers() {
+  for (tsq::DevBuf *d : {&seqs, &codes, &pairs, &tasks, &wtasks, &res, &bnd, &planes, &plane_off, &aln, &aln_off,
+                         &shape_g, &shape_r, &counters, &lut, &matrix, &overflow, &rerun_tasks, &rerun_wtasks, &ccodes,
+                         &clut, &cmatrix})
+    d->release();
+}
+
 tsq_batch::~tsq_batch() {
+  release_device_buffers();
   if (ev_fetch) cudaEventDestroy(ev_fetch);
   if (ev_fork) cudaEventDestroy(ev_fork);
   if (ev_join) cudaEventDestroy(ev_join);
@@ -319,6 +387,7 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
     b->graph = nullptr;
   }
   if (b->stream && b->device != dev) {
+    b->release_device_buffers();
     cudaStreamDestroy(b->stream);
     b->stream = nullptr;
     if (b->side) cudaStreamDestroy(b->side);
@@ -412,9 +481,9 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   // Score batches also get class codes for the int16x2 fill.
   b->classes = b->out_mode == kOutScore && p->lane != TSQ_LANE_I32;
   if (!b->input_owner) {
-    TSQ_TRY(b->seqs.ensure(size_t(seqs_len) + 128));
-    TSQ_TRY(b->codes.ensure(size_t(seqs_len) + 128));
-    if (b->classes) TSQ_TRY(b->ccodes.ensure(size_t(seqs_len) + 128));
+    TSQ_TRY(b->seqs.ensure(size_t(seqs_len) + 128, b->stream));
+    TSQ_TRY(b->codes.ensure(size_t(seqs_len) + 128, b->stream));
+    if (b->classes) TSQ_TRY(b->ccodes.ensure(size_t(seqs_len) + 128, b->stream));
     if (seqs_len > 0 && !segmented)
       TSQ_TRY(cudaMemcpyAsync(b->seqs.p, seqs, size_t(seqs_len), cudaMemcpyHostToDevice, b->stream));
   }
@@ -693,32 +762,32 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   build_lut(sc, lut);
   // (seqs and codes were sized above: staged code chunks read up to 64
   // bytes past a sequence, hence the padding.)
-  TSQ_TRY(b->pairs.ensure(sizeof(PairDev) * size_t(n)));
-  TSQ_TRY(b->tasks.ensure(sizeof(int32_t) * size_t(n)));
-  TSQ_TRY(b->res.ensure(sizeof(ResultDev) * size_t(n)));
-  TSQ_TRY(b->bnd.ensure(size_t(bnd_total)));
-  TSQ_TRY(b->wtasks.ensure(sizeof(int2) * std::max<size_t>(1, wt_sorted.size())));
-  TSQ_TRY(b->counters.ensure(sizeof(int32_t) * (b->launches.size() + 2)));
-  TSQ_TRY(b->shape_g.ensure(sizeof(int32_t) * size_t(n)));
-  TSQ_TRY(b->shape_r.ensure(sizeof(int32_t) * size_t(n)));
+  TSQ_TRY(b->pairs.ensure(sizeof(PairDev) * size_t(n), b->stream));
+  TSQ_TRY(b->tasks.ensure(sizeof(int32_t) * size_t(n), b->stream));
+  TSQ_TRY(b->res.ensure(sizeof(ResultDev) * size_t(n), b->stream));
+  TSQ_TRY(b->bnd.ensure(size_t(bnd_total), b->stream));
+  TSQ_TRY(b->wtasks.ensure(sizeof(int2) * std::max<size_t>(1, wt_sorted.size()), b->stream));
+  TSQ_TRY(b->counters.ensure(sizeof(int32_t) * (b->launches.size() + 2), b->stream));
+  TSQ_TRY(b->shape_g.ensure(sizeof(int32_t) * size_t(n), b->stream));
+  TSQ_TRY(b->shape_r.ensure(sizeof(int32_t) * size_t(n), b->stream));
   if (n_checked > 0) {
-    TSQ_TRY(b->overflow.ensure(sizeof(int32_t) * size_t(n)));
-    TSQ_TRY(b->rerun_tasks.ensure(sizeof(int32_t) * size_t(n_checked)));
-    TSQ_TRY(b->rerun_wtasks.ensure(sizeof(int2) * size_t(n_checked)));
+    TSQ_TRY(b->overflow.ensure(sizeof(int32_t) * size_t(n), b->stream));
+    TSQ_TRY(b->rerun_tasks.ensure(sizeof(int32_t) * size_t(n_checked), b->stream));
+    TSQ_TRY(b->rerun_wtasks.ensure(sizeof(int2) * size_t(n_checked), b->stream));
   }
   TSQ_TRY(b->rerun_h.ensure(sizeof(int32_t)));
-  TSQ_TRY(b->lut.ensure(256));
-  TSQ_TRY(b->matrix.ensure(kLetters * kLetters));
+  TSQ_TRY(b->lut.ensure(256, b->stream));
+  TSQ_TRY(b->matrix.ensure(kLetters * kLetters, b->stream));
   if (b->classes) {
-    TSQ_TRY(b->clut.ensure(256));
-    TSQ_TRY(b->cmatrix.ensure(kLetters * kLetters));
+    TSQ_TRY(b->clut.ensure(256, b->stream));
+    TSQ_TRY(b->cmatrix.ensure(kLetters * kLetters, b->stream));
   }
   TSQ_TRY(b->res_h.ensure(sizeof(ResultDev) * size_t(n)));
   if (b->out_mode == kOutTrace) {
-    TSQ_TRY(b->planes.ensure(size_t(plane_total)));
-    TSQ_TRY(b->plane_off.ensure(sizeof(int64_t) * size_t(n)));
-    TSQ_TRY(b->aln.ensure(size_t(b->aln_bytes)));
-    TSQ_TRY(b->aln_off.ensure(sizeof(int64_t) * size_t(n)));
+    TSQ_TRY(b->planes.ensure(size_t(plane_total), b->stream));
+    TSQ_TRY(b->plane_off.ensure(sizeof(int64_t) * size_t(n), b->stream));
+    TSQ_TRY(b->aln.ensure(size_t(b->aln_bytes), b->stream));
+    TSQ_TRY(b->aln_off.ensure(sizeof(int64_t) * size_t(n), b->stream));
     TSQ_TRY(b->aln_h.ensure(size_t(b->aln_bytes)));
   }
   cudaStream_t st = b->stream;

@@ -13,7 +13,13 @@ namespace tsq {
 struct DevBuf {
   void *p = nullptr;
   size_t cap = 0;
-  cudaError_t ensure(size_t bytes);
+  cudaStream_t owner = nullptr;  // stream of a stream-ordered allocation
+  // Grows the buffer (contents are not kept).  With a stream, the old
+  // buffer is freed and the new one allocated in stream order, so growing
+  // one batch's buffers does not wait for other streams' work.
+  cudaError_t ensure(size_t bytes, cudaStream_t stream = nullptr);
+  // Frees in the owner stream's order when there is one; the owner stream
+  // must still exist.
   void release();
   template <class T>
   T *as() const {
@@ -135,6 +141,8 @@ struct tsq_batch {
   tsq::DevBuf ccodes, clut, cmatrix;
   bool classes = false;
   tsq::PinBuf res_h, aln_h, rerun_h;
+  // Frees every device buffer (in stream order) before the streams go.
+  void release_device_buffers();
   int64_t n_checked = 0;
   int32_t checked_begin = 0;
 
