@@ -359,6 +359,39 @@ def test_chunked_call_equals_single_plan(output, local):
         assert np.array_equal(got.table["b_end"][idx], o["b_end"])
 
 
+def _call_batch(seqs_ptr, seqs_len, tab, output="score"):
+    raw = np.zeros(len(tab), dtype=N.RESULT_DTYPE)
+    p, keep = N.make_params(output=output)
+    rc = N.lib().tsq_align_batch(seqs_ptr, seqs_len, tab.ctypes.data, len(tab), ctypes.byref(p),
+                                 ctypes.byref(A._opts()), raw.ctypes.data)
+    return rc, raw
+
+
+@pytest.mark.parametrize("output", ["score", "identity"])
+def test_chunked_call_page_locked_input(output):
+    """Page-locked residues go up whole while the first chunk is planned;
+    the results equal those of the same call on pageable memory, including
+    a pair with an invalid residue in the last chunk."""
+    torch = pytest.importorskip("torch")
+    ps = W.uneven_pairs(n_pairs=40000, seed=14)
+    seqs, tab = A._as_inputs(ps)
+    seqs = seqs.copy()
+    seqs[int(tab["a_off"][35000]) + 3] = ord("#")  # pair 35000 is in the last chunk
+    pinned = torch.from_numpy(seqs).pin_memory()
+    rc_p, got = _call_batch(pinned.data_ptr(), len(seqs), tab, output)
+    rc_h, want = _call_batch(seqs.ctypes.data, len(seqs), tab, output)
+    assert rc_p == rc_h == N.E_INVALID_RESIDUE
+    assert got["status"][35000] == N.E_INVALID_RESIDUE
+    for f in ("score", "n_ident", "n_cols", "status"):
+        assert np.array_equal(got[f], want[f]), f
+    bad = tab.copy()
+    bad["b_len"][39000] = -1
+    rc, _ = _call_batch(pinned.data_ptr(), len(seqs), bad, output)
+    assert rc == N.E_INVALID_ARG
+    rc, again = _call_batch(pinned.data_ptr(), len(seqs), tab, output)
+    assert rc == N.E_INVALID_RESIDUE and np.array_equal(again["score"], want["score"])
+
+
 def test_chunked_call_reports_the_first_bad_pair():
     ps = W.uneven_pairs(n_pairs=40000, seed=13)
     seqs, tab = A._as_inputs(ps)

@@ -1,5 +1,6 @@
 // api.cpp -- the extern "C" entry points declared in include/tweakseq_gb300.h.
 #include <algorithm>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <exception>
@@ -22,6 +23,11 @@ struct ThreadCache {
   cudaStream_t input_stream = nullptr;
   std::vector<cudaEvent_t> seg_events;
   int input_dev = -1;
+  // A chunked call's cost order: each pair's cost bin, the pairs in cost
+  // order and their input positions.
+  std::vector<uint8_t> order_bin;
+  std::vector<tsq_pair_desc> order_pairs;
+  std::vector<int32_t> order_index;
   ~ThreadCache() {
     for (cudaEvent_t e : seg_events) cudaEventDestroy(e);
     if (input_stream) cudaStreamDestroy(input_stream);
@@ -58,27 +64,35 @@ int guarded(F &&f) {
   }
 }
 
-// A large score or identity call runs as a few chunks of consecutive pairs,
-// each planned by its own batch object and run on its own stream.
-// - Chunks grow in size (1/6, 2/6, 3/6 of the pairs with three chunks), so
-//   the first starts early and each later one is planned on the host while
-//   the earlier ones run.  (Two to four chunks measured within 2 % of each
-//   other on the 100,000-pair batch; three is the best of them.)
-// - The residues go up in segments on an input stream: segment k holds what
-//   chunk k reads beyond the earlier segments, so a chunk waits only for the
-//   residues up to its own.
-// - The chunks' persistent launches fill each other's tails on the device.
-// Each pair's result does not depend on the chunking.
+// A large score or identity call runs as a few chunks, each planned by its
+// own batch object and run on its own stream; each later chunk is planned on
+// the host while the earlier ones run, and the chunks' persistent launches
+// fill each other's tails on the device.  Each pair's result does not depend
+// on the chunking.  Two ways of cutting and feeding the chunks:
+// - Input the device can read in place (page-locked, 16-byte aligned): one
+//   kernel encodes the residues straight from host memory while the host
+//   plans the first chunk.  Chunks are cut by cost: chunk 0 takes the
+//   costliest tenth of the pairs (cells, binned at four steps per octave, in
+//   input order within a bin), chunk 1 the next three tenths, chunk 2 the
+//   rest.  The first plan is small, its long pairs keep the device busy
+//   while the host plans the rest, and the last chunk -- launched last --
+//   holds the short pairs, so the call ends with a short tail.  Results go
+//   back to their input positions.  (Chunks of consecutive pairs left the
+//   longest pairs of the last chunk to start late: 5.4 ms of fills for
+//   4.97 ms of work on the 100,000-pair batch.)
+// - Other (pageable) input: chunks of consecutive pairs growing in size
+//   (1/6, 2/6, 3/6 with three chunks), the residues uploaded in segments on
+//   an input stream -- segment k holds what chunk k reads beyond the earlier
+//   segments -- so a chunk waits only for the residues up to its own, and
+//   the host copies the next segment while the device fills earlier chunks.
 int align_in_chunks(ThreadCache &c, tsq_batch *e, const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *pairs,
                     int64_t n, const tsq_params *p, const tsq_batch_opts *opts, tsq_result *out) {
+  if (n > INT32_MAX / 2) return TSQ_E_TOO_LARGE;
   const int K = int(std::min<int64_t>(kMaxChunks, n / kChunkPairs));
   while (int(c.chunk_engines.size()) < K - 1) c.chunk_engines.emplace_back(new tsq_batch());
   std::vector<tsq_batch *> eng(static_cast<size_t>(K));
   eng[0] = e;
   for (int k = 1; k < K; ++k) eng[size_t(k)] = c.chunk_engines[size_t(k - 1)].get();
-  // Chunk k ends at n * (1 + 2 + ... + (k+1)) / (1 + 2 + ... + K).
-  const int64_t tri = int64_t(K) * (K + 1) / 2;
-  auto begin = [&](int k) { return n * (int64_t(k) * (k + 1) / 2) / tri; };
   int dev = 0;
   if (opts && opts->device >= 0)
     dev = opts->device;
@@ -99,27 +113,64 @@ int align_in_chunks(ThreadCache &c, tsq_batch *e, const uint8_t *seqs, int64_t s
     c.seg_events.push_back(ev);
   }
   const tsq_batch_opts o{dev, 0, opts ? opts->autotune : 0, 0};
+
+  cudaPointerAttributes attr{};
+  const bool in_place = seqs_len > 0 && cudaPointerGetAttributes(&attr, seqs) == cudaSuccess &&
+                        attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr &&
+                        reinterpret_cast<uintptr_t>(attr.devicePointer) % 16 == 0;
+  cudaGetLastError();  // (a pointer CUDA does not know leaves an error behind)
+  int rc = TSQ_OK;
+  if (in_place) {  // the encode runs while the host orders and plans
+    rc = tsq::input_prepare(e, seqs_len, p, &o);
+    if (rc == TSQ_OK)
+      rc = tsq::input_encode_mapped(e, static_cast<const uint8_t *>(attr.devicePointer), c.input_stream);
+    if (rc == TSQ_OK && cudaEventRecord(c.seg_events[0], c.input_stream) != cudaSuccess) rc = TSQ_E_CUDA;
+  }
+
+  // Chunk k covers positions [cut[k], cut[k+1]) of the chunk order: the
+  // input order, or (in place) the cost order held in c.order_pairs with the
+  // input index of each position in c.order_index.
+  std::vector<int64_t> cut(static_cast<size_t>(K) + 1);
   int64_t cells = 0;
-  for (int64_t k = 0; k < n; ++k) cells += int64_t(std::max(pairs[k].a_len, 0)) * std::max(pairs[k].b_len, 0);
-  int launched = 0, rc = TSQ_OK;
-  int64_t uploaded = 0;  // residues [0, uploaded) are on their way
+  const tsq_pair_desc *chunk_pairs = pairs;
+  const int32_t *chunk_index = nullptr;
+  if (in_place) {
+    static const double kCut3[] = {0.0, 0.1, 0.4, 1.0}, kCut2[] = {0.0, 0.2, 1.0};
+    for (int k = 0; k <= K; ++k) cut[size_t(k)] = int64_t(double(n) * (K == 3 ? kCut3[k] : kCut2[k]));
+    cut[size_t(K)] = n;
+    c.order_pairs.resize(size_t(n));
+    c.order_index.resize(size_t(n));
+    cells = tsq::cost_order(pairs, n, c.order_bin, c.order_pairs.data(), c.order_index.data());
+    chunk_pairs = c.order_pairs.data();
+    chunk_index = c.order_index.data();
+  } else {
+    // Chunk k ends at n * (1 + 2 + ... + (k+1)) / (1 + 2 + ... + K).
+    const int64_t tri = int64_t(K) * (K + 1) / 2;
+    for (int k = 0; k <= K; ++k) cut[size_t(k)] = n * (int64_t(k) * (k + 1) / 2) / tri;
+    for (int64_t k = 0; k < n; ++k) cells += int64_t(std::max(pairs[k].a_len, 0)) * std::max(pairs[k].b_len, 0);
+  }
+
+  int launched = 0;
+  int64_t uploaded = 0;  // (pageable) residues [0, uploaded) are on their way
   for (int k = 0; k < K && rc == TSQ_OK; ++k) {
-    const tsq_pair_desc *pk = pairs + begin(k);
-    const int64_t nk = begin(k + 1) - begin(k);
+    const int64_t b0 = cut[size_t(k)], nk = cut[size_t(k) + 1] - b0;
+    const tsq_pair_desc *pk = chunk_pairs + b0;
     rc = tsq::batch_plan_chunk(eng[size_t(k)], k == 0 ? nullptr : e, seqs, seqs_len, pk, nk, p, &o, n, cells, true);
     if (rc != TSQ_OK) break;
-    // This chunk's residue segment: whole 16-byte blocks, plus the 64 bytes
-    // past a sequence end that the fills' staging reads; the last chunk
-    // takes the rest of the buffer.
-    int64_t hi = uploaded;
-    for (int64_t q = 0; q < nk; ++q)
-      hi = std::max({hi, pk[q].a_off + pk[q].a_len, pk[q].b_off + pk[q].b_len});
-    hi = k == K - 1 ? seqs_len : std::min(seqs_len, (hi + 64 + 15) / 16 * 16);
-    rc = tsq::input_segment(e, seqs, uploaded, hi, c.input_stream);
-    if (rc == TSQ_OK && cudaEventRecord(c.seg_events[size_t(k)], c.input_stream) != cudaSuccess) rc = TSQ_E_CUDA;
-    if (rc != TSQ_OK) break;
-    uploaded = hi;
-    eng[size_t(k)]->input_ready = c.seg_events[size_t(k)];
+    if (!in_place) {
+      // This chunk's segment: whole 16-byte blocks, plus the 64 bytes past
+      // a sequence end that the fills' staging reads; the last chunk takes
+      // the rest of the buffer.
+      int64_t hi = uploaded;
+      for (int64_t q = 0; q < nk; ++q)
+        hi = std::max({hi, pk[q].a_off + pk[q].a_len, pk[q].b_off + pk[q].b_len});
+      hi = k == K - 1 ? seqs_len : std::min(seqs_len, (hi + 64 + 15) / 16 * 16);
+      rc = tsq::input_segment(e, seqs, uploaded, hi, c.input_stream);
+      if (rc == TSQ_OK && cudaEventRecord(c.seg_events[size_t(k)], c.input_stream) != cudaSuccess) rc = TSQ_E_CUDA;
+      if (rc != TSQ_OK) break;
+      uploaded = hi;
+    }
+    eng[size_t(k)]->input_ready = c.seg_events[in_place ? 0 : size_t(k)];
     rc = tsq::batch_run_async(eng[size_t(k)]);
     if (rc == TSQ_OK) ++launched;
   }
@@ -128,11 +179,20 @@ int align_in_chunks(ThreadCache &c, tsq_batch *e, const uint8_t *seqs, int64_t s
     const int sync_rc = tsq::batch_sync(eng[size_t(k)]);
     if (status != TSQ_OK && status != TSQ_E_INVALID_RESIDUE) continue;  // drain the rest, report the first error
     int r = sync_rc;
-    if (r == TSQ_OK) r = tsq::batch_results(eng[size_t(k)], out + begin(k));
+    if (r == TSQ_OK)
+      r = chunk_index ? tsq::batch_results(eng[size_t(k)], out, chunk_index + cut[size_t(k)])
+                      : tsq::batch_results(eng[size_t(k)], out + cut[size_t(k)]);
     if (r != TSQ_OK && (status == TSQ_OK || r != TSQ_E_INVALID_RESIDUE)) status = r;
   }
-  // The input stream's copies read the caller's residues: done before return.
+  // The input stream reads the caller's residues: done before return.
   cudaStreamSynchronize(c.input_stream);
+  e->input_prepared = false;
+  if (in_place && (rc == TSQ_E_INVALID_ARG || rc == TSQ_E_TOO_LARGE)) {
+    // A chunk in cost order found a bad pair: report what one plan of the
+    // whole call reports (the first bad pair in input order).
+    const int whole = tsq::batch_plan(e, seqs, seqs_len, pairs, n, p, &o, false);
+    if (whole != TSQ_OK) status = whole;
+  }
   return status;
 }
 

@@ -10,6 +10,7 @@
 #include "engine.h"
 
 #include <algorithm>
+#include <array>
 #include <cstdlib>
 #include <cstring>
 #include <atomic>
@@ -239,6 +240,13 @@ int parallel_for(int64_t n, F &&f) {
   return 1;
 }
 
+// Runs task(i) for i in [0, tasks) on the worker pool, or in turn on the
+// calling thread when the pool is busy.
+void run_slices(int tasks, const std::function<void(int)> &task) {
+  if (tasks > 1 && WorkerPool::get().run(tasks, task)) return;
+  for (int i = 0; i < tasks; ++i) task(i);
+}
+
 // Stable LSD radix sort by key (ascending) in 11-bit digits over the low
 // `bits` bits; a digit that is the same for every record costs only its
 // count.  tmp is scratch (grown to the size of a when smaller).
@@ -323,6 +331,10 @@ namespace {
 int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t seqs_len,
               const tsq_pair_desc *pairs, int64_t n, const tsq_params *p, const tsq_batch_opts *opts, bool plain,
               int64_t call_pairs, int64_t call_cells, bool segmented);
+int prepare_object(tsq_batch *b, const tsq_params *p, const tsq_batch_opts *opts, Scheme *sc, int *sms);
+int out_mode_of(const tsq_params *p) {
+  return p->output == TSQ_OUT_ALIGNMENT ? kOutTrace : (p->output == TSQ_OUT_IDENTITY ? kOutIdent : kOutScore);
+}
 }  // namespace
 
 int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *pairs, int64_t n,
@@ -352,30 +364,57 @@ int input_segment(const tsq_batch *owner, const uint8_t *seqs, int64_t begin, in
   return TSQ_OK;
 }
 
+int input_encode_mapped(const tsq_batch *owner, const uint8_t *src_dev, cudaStream_t stream) {
+  if (!owner || !src_dev || reinterpret_cast<uintptr_t>(src_dev) % 16 != 0) return TSQ_E_INVALID_ARG;
+  TSQ_TRY(launch_encode(src_dev, owner->seqs_len, owner->lut.as<uint8_t>(), owner->codes.as<uint8_t>(),
+                        owner->classes ? owner->clut.as<uint8_t>() : nullptr,
+                        owner->classes ? owner->ccodes.as<uint8_t>() : nullptr, stream));
+  return TSQ_OK;
+}
+
+int input_prepare(tsq_batch *owner, int64_t seqs_len, const tsq_params *p, const tsq_batch_opts *opts) {
+  if (!owner || !p || seqs_len < 0) return TSQ_E_INVALID_ARG;
+  Scheme sc;
+  int sms = 0;
+  int rc = prepare_object(owner, p, opts, &sc, &sms);
+  if (rc) return rc;
+  cudaStream_t st = owner->stream;
+  owner->classes = out_mode_of(p) == kOutScore && p->lane != TSQ_LANE_I32;
+  owner->seqs_len = seqs_len;
+  TSQ_TRY(owner->seqs.ensure(size_t(seqs_len) + 128, st));
+  TSQ_TRY(owner->codes.ensure(size_t(seqs_len) + 128, st));
+  if (owner->classes) TSQ_TRY(owner->ccodes.ensure(size_t(seqs_len) + 128, st));
+  TSQ_TRY(owner->lut.ensure(256, st));
+  uint8_t lut[256], clut[256];
+  build_lut(sc, lut);
+  TSQ_TRY(cudaMemcpyAsync(owner->lut.p, lut, 256, cudaMemcpyHostToDevice, st));
+  if (owner->classes) {
+    TSQ_TRY(owner->clut.ensure(256, st));
+    build_class_lut(sc, clut);
+    TSQ_TRY(cudaMemcpyAsync(owner->clut.p, clut, 256, cudaMemcpyHostToDevice, st));
+  }
+  // The buffers and tables are then usable from the input stream.
+  TSQ_TRY(cudaStreamSynchronize(st));
+  owner->input_prepared = true;
+  return TSQ_OK;
+}
+
 namespace {
-int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t seqs_len,
-              const tsq_pair_desc *pairs, int64_t n, const tsq_params *p, const tsq_batch_opts *opts, bool plain,
-              int64_t call_pairs, int64_t call_cells, bool segmented) {
-  if (!b || !p || n < 0 || seqs_len < 0) return TSQ_E_INVALID_ARG;
-  b->input_owner = owner;
-  b->input_segmented = segmented;
-  if (n > 0 && !pairs) return TSQ_E_INVALID_ARG;
-  if (seqs_len > 0 && !seqs && !owner) return TSQ_E_INVALID_ARG;
-  if (n > INT32_MAX / 2) return TSQ_E_TOO_LARGE;
+// Checks the parameters, builds the scheme and readies the object for a new
+// plan on its device: drops an old graph, (re)creates its streams and events.
+int prepare_object(tsq_batch *b, const tsq_params *p, const tsq_batch_opts *opts, Scheme *sc, int *sms) {
   if (p->gap_open < 0 || p->gap_extend < 0 || p->gap_open > 1000000 || p->gap_extend > 1000000)
     return TSQ_E_INVALID_ARG;
   if (p->mode != TSQ_GLOBAL && p->mode != TSQ_LOCAL) return TSQ_E_INVALID_ARG;
   if (p->output < TSQ_OUT_SCORE || p->output > TSQ_OUT_ALIGNMENT) return TSQ_E_INVALID_ARG;
   if (p->lane < TSQ_LANE_AUTO || p->lane > TSQ_LANE_I32) return TSQ_E_INVALID_ARG;
-  Scheme sc;
-  int rc = build_scheme(p, &sc);
+  int rc = build_scheme(p, sc);
   if (rc) return rc;
 
   int dev = opts && opts->device >= 0 ? opts->device : -1;
   if (dev < 0) TSQ_TRY(cudaGetDevice(&dev));
   TSQ_TRY(cudaSetDevice(dev));
-  int sms = 0;
-  TSQ_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  TSQ_TRY(cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev));
 
   // A replanned object drops its old graph.
   if (b->gexec) {
@@ -401,10 +440,30 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   for (auto &e : b->ev)
     if (!e) TSQ_TRY(cudaEventCreate(&e));
   if (!b->ev_encoded) TSQ_TRY(cudaEventCreateWithFlags(&b->ev_encoded, cudaEventDisableTiming));
+  return TSQ_OK;
+}
+
+int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t seqs_len,
+              const tsq_pair_desc *pairs, int64_t n, const tsq_params *p, const tsq_batch_opts *opts, bool plain,
+              int64_t call_pairs, int64_t call_cells, bool segmented) {
+  if (!b) return TSQ_E_INVALID_ARG;
+  // The flag holds for this plan only, whatever it returns.
+  const bool prepared = b->input_prepared;
+  b->input_prepared = false;
+  if (!p || n < 0 || seqs_len < 0) return TSQ_E_INVALID_ARG;
+  b->input_owner = owner;
+  b->input_segmented = segmented;
+  if (n > 0 && !pairs) return TSQ_E_INVALID_ARG;
+  if (seqs_len > 0 && !seqs && !owner) return TSQ_E_INVALID_ARG;
+  if (n > INT32_MAX / 2) return TSQ_E_TOO_LARGE;
+  Scheme sc;
+  int sms = 0;
+  int rc = prepare_object(b, p, opts, &sc, &sms);
+  if (rc) return rc;
 
   b->scheme = sc;
   b->params = *p;
-  b->out_mode = p->output == TSQ_OUT_ALIGNMENT ? kOutTrace : (p->output == TSQ_OUT_IDENTITY ? kOutIdent : kOutScore);
+  b->out_mode = out_mode_of(p);
   b->local = p->mode == TSQ_LOCAL;
   b->use_graph = opts ? opts->use_graph != 0 : false;
   b->autotune = opts ? opts->autotune != 0 : false;
@@ -797,12 +856,14 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
     TSQ_TRY(cudaMemcpyAsync(b->wtasks.p, wt_sorted.data(), sizeof(int2) * wt_sorted.size(), cudaMemcpyHostToDevice,
                             st));
   }
-  TSQ_TRY(cudaMemcpyAsync(b->lut.p, lut, 256, cudaMemcpyHostToDevice, st));
+  // (An input set up by input_prepare has its code tables on the device
+  // already, read by encode kernels that may be running now.)
+  if (!prepared) TSQ_TRY(cudaMemcpyAsync(b->lut.p, lut, 256, cudaMemcpyHostToDevice, st));
   TSQ_TRY(cudaMemcpyAsync(b->matrix.p, sc.score, kLetters * kLetters, cudaMemcpyHostToDevice, st));
   uint8_t clut[256];
   if (b->classes) {
     build_class_lut(sc, clut);
-    TSQ_TRY(cudaMemcpyAsync(b->clut.p, clut, 256, cudaMemcpyHostToDevice, st));
+    if (!prepared) TSQ_TRY(cudaMemcpyAsync(b->clut.p, clut, 256, cudaMemcpyHostToDevice, st));
     TSQ_TRY(cudaMemcpyAsync(b->cmatrix.p, sc.cscore, size_t(sc.nclasses) * sc.nclasses, cudaMemcpyHostToDevice,
                             st));
   }
@@ -1018,13 +1079,94 @@ int batch_fetch_query(tsq_batch *b) {
   return cuda_status(e);
 }
 
-int batch_collect(tsq_batch *b, int64_t begin, int64_t count, tsq_result *out) {
+int64_t cost_order(const tsq_pair_desc *pairs, int64_t n, std::vector<uint8_t> &bin, tsq_pair_desc *out_pairs,
+                   int32_t *out_index) {
+  if (n <= 0) return 0;
+  bin.resize(size_t(n));
+  // Fixed slices, the same in both passes.
+  const int slices = int(std::min<int64_t>({8, int64_t(WorkerPool::get().workers()) + 1, (n + 8191) / 8192}));
+  const int64_t step = (n + slices - 1) / slices;
+  std::vector<std::array<int64_t, 256>> hist(static_cast<size_t>(slices));
+  std::vector<int64_t> cells(static_cast<size_t>(slices), 0);
+  run_slices(slices, [&](int s) {
+    std::array<int64_t, 256> &h = hist[size_t(s)];
+    h.fill(0);
+    int64_t c = 0;
+    for (int64_t k = int64_t(s) * step, e = std::min(n, k + step); k < e; ++k) {
+      const int64_t ck = int64_t(std::max(pairs[k].a_len, 0)) * std::max(pairs[k].b_len, 0);
+      c += ck;
+      const int bw = ck > 0 ? 64 - __builtin_clzll(uint64_t(ck)) : 0;
+      const int b = 4 * bw + (bw >= 3 ? int((uint64_t(ck) >> (bw - 3)) & 3) : 0);
+      bin[size_t(k)] = uint8_t(b);
+      ++h[size_t(b)];
+    }
+    cells[size_t(s)] = c;
+  });
+  // Position of each (bin, slice) run: bins descending, slices in order.
+  int64_t acc = 0;
+  for (int b = 255; b >= 0; --b)
+    for (int s = 0; s < slices; ++s) {
+      const int64_t c = hist[size_t(s)][size_t(b)];
+      hist[size_t(s)][size_t(b)] = acc;
+      acc += c;
+    }
+  run_slices(slices, [&](int s) {
+    std::array<int64_t, 256> &next = hist[size_t(s)];
+    for (int64_t k = int64_t(s) * step, e = std::min(n, k + step); k < e; ++k) {
+      const int64_t r = next[bin[size_t(k)]]++;
+      out_pairs[r] = pairs[k];
+      out_index[r] = int32_t(k);
+    }
+  });
+  int64_t total = 0;
+  for (int64_t c : cells) total += c;
+  return total;
+}
+
+int batch_collect(tsq_batch *b, int64_t begin, int64_t count, tsq_result *out, const int32_t *dst) {
   if (!b || begin < 0 || count < 0 || begin + count > b->n || (count > 0 && !out)) return TSQ_E_INVALID_ARG;
   const ResultDev *r = b->res_h.as<ResultDev>();
+  if (b->out_mode != kOutTrace && count >= 16384) {
+    // Parallel over the pairs (a scattered collect is bound by its writes).
+    // The status is what the serial loop below returns: the last pair's
+    // error other than a residue error, else a residue error, else OK.
+    struct Part {
+      int last = TSQ_OK;
+      bool residue = false;
+    };
+    Part parts[8];
+    parallel_for(count, [&](int64_t lo, int64_t hi, int slot) {
+      Part pt;
+      for (int64_t q = lo; q < hi; ++q) {
+        const ResultDev &d = r[begin + q];
+        tsq_result &o = dst ? out[dst[q]] : out[q];
+        o.score = d.score;
+        o.a_begin = d.a_begin;
+        o.a_end = d.a_end;
+        o.b_begin = d.b_begin;
+        o.b_end = d.b_end;
+        o.n_ident = d.n_ident;
+        o.n_cols = d.n_cols;
+        o.status = d.status;
+        o.aln_a = o.aln_b = nullptr;
+        if (d.status == TSQ_E_INVALID_RESIDUE)
+          pt.residue = true;
+        else if (d.status != TSQ_OK)
+          pt.last = d.status;
+      }
+      parts[slot] = pt;
+    });
+    int rc = TSQ_OK;
+    for (const Part &pt : parts) {
+      if (pt.residue && rc == TSQ_OK) rc = TSQ_E_INVALID_RESIDUE;
+      if (pt.last != TSQ_OK) rc = pt.last;
+    }
+    return rc;
+  }
   int rc = TSQ_OK;
   for (int64_t q = 0; q < count; ++q) {
     const int64_t k = begin + q;
-    tsq_result &o = out[q];
+    tsq_result &o = dst ? out[dst[q]] : out[q];
     const ResultDev &d = r[k];
     o.score = d.score;
     o.a_begin = d.a_begin;
@@ -1063,12 +1205,14 @@ int batch_collect(tsq_batch *b, int64_t begin, int64_t count, tsq_result *out) {
   return rc;
 }
 
-int batch_results(tsq_batch *b, tsq_result *out) {
+int batch_results(tsq_batch *b, tsq_result *out) { return batch_results(b, out, nullptr); }
+
+int batch_results(tsq_batch *b, tsq_result *out, const int32_t *dst) {
   if (!b || (b->n > 0 && !out)) return TSQ_E_INVALID_ARG;
   int rc = batch_fetch_async(b);
   if (rc) return rc;
   TSQ_TRY(cudaStreamSynchronize(b->stream));
-  return batch_collect(b, 0, b->n, out);
+  return batch_collect(b, 0, b->n, out, dst);
 }
 
 int64_t batch_device_bytes(const tsq_batch *b) {

@@ -134,6 +134,9 @@ struct tsq_batch {
   // fills wait on input_ready, the event after this chunk's segment.
   bool input_segmented = false;
   cudaEvent_t input_ready = nullptr;
+  // Set by input_prepare: the next plan keeps the residue buffers and code
+  // tables it set up.
+  bool input_prepared = false;
 
   tsq::DevBuf seqs, codes, pairs, tasks, wtasks, res, bnd, planes, plane_off, aln, aln_off, shape_g, shape_r, counters,
       lut, matrix, overflow, rerun_tasks, rerun_wtasks;
@@ -168,13 +171,32 @@ int batch_plan_chunk(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, 
 // encodes them, on `stream`; begin is a multiple of 16.  The owner must be
 // planned (its code tables are on the device).
 int input_segment(const tsq_batch *owner, const uint8_t *seqs, int64_t begin, int64_t end, cudaStream_t stream);
+// Readies the first chunk's object of a call to receive seqs_len residues
+// before it is planned: its device buffers, and the code tables for the
+// parameters, usable from any stream on return.  Its next plan (with
+// segmented input) keeps them, so input_segment can upload and encode the
+// whole input while the host plans.
+int input_prepare(tsq_batch *owner, int64_t seqs_len, const tsq_params *p, const tsq_batch_opts *opts);
+// Encodes the owner's whole input (owner->seqs_len residues) on `stream`
+// straight from memory the device reads in place (a page-locked host buffer
+// through its device address, 16-byte aligned); the owner keeps no copy of
+// the residues, which score and identity fills do not read.
+int input_encode_mapped(const tsq_batch *owner, const uint8_t *src_dev, cudaStream_t stream);
 int batch_run_async(tsq_batch *b);
 int batch_sync(tsq_batch *b);
 int batch_results(tsq_batch *b, tsq_result *out);
+// The same, pair q's result going to out[dst[q]].
+int batch_results(tsq_batch *b, tsq_result *out, const int32_t *dst);
 // Asynchronous read-back: enqueue the copies, poll, then convert a range.
 int batch_fetch_async(tsq_batch *b);
 int batch_fetch_query(tsq_batch *b);  // TSQ_OK when the copies landed, TSQ_E_PENDING before
-int batch_collect(tsq_batch *b, int64_t begin, int64_t count, tsq_result *out);
+int batch_collect(tsq_batch *b, int64_t begin, int64_t count, tsq_result *out, const int32_t *dst = nullptr);
+// Orders a call's pairs by cost, costliest first: cells binned at four steps
+// per octave, bins descending, input order within a bin.  Writes the pairs
+// in that order and each one's input index; returns the total cells.
+// Parallel on the worker pool; `bin` is scratch.
+int64_t cost_order(const tsq_pair_desc *pairs, int64_t n, std::vector<uint8_t> &bin, tsq_pair_desc *out_pairs,
+                   int32_t *out_index);
 int64_t batch_device_bytes(const tsq_batch *b);
 int cuda_status(cudaError_t e);
 }  // namespace tsq
