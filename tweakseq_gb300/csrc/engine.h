@@ -14,10 +14,11 @@ struct DevBuf {
   void *p = nullptr;
   size_t cap = 0;
   cudaStream_t owner = nullptr;  // stream of a stream-ordered allocation
-  // Grows the buffer (contents are not kept).  With a stream, the old
-  // buffer is freed and the new one allocated in stream order, so growing
-  // one batch's buffers does not wait for other streams' work.
-  cudaError_t ensure(size_t bytes, cudaStream_t stream = nullptr);
+  // Grows the buffer (contents are not kept).  With a stream, a buffer below
+  // async_max bytes is freed and allocated in stream order, so growing one
+  // batch's buffers does not wait for other streams' work; larger ones come
+  // from cudaMalloc (stream-ordered allocation maps memory far more slowly).
+  cudaError_t ensure(size_t bytes, cudaStream_t stream = nullptr, size_t async_max = size_t(256) << 20);
   // Frees in the owner stream's order when there is one; the owner stream
   // must still exist.
   void release();
@@ -144,6 +145,11 @@ struct tsq_batch {
   tsq::DevBuf ccodes, clut, cmatrix;
   bool classes = false;
   tsq::PinBuf res_h, aln_h, rerun_h;
+  // Device buffers below this size grow in stream order.  A serving slot,
+  // whose growth must not wait for the other slots' kernels, takes every
+  // size in stream order; a one-off large batch prefers cudaMalloc's faster
+  // mapping of its traceback planes.
+  size_t async_max = size_t(256) << 20;
   // Frees every device buffer (in stream order) before the streams go.
   void release_device_buffers();
   int64_t n_checked = 0;

@@ -20,6 +20,7 @@
 // the other requests of a tick nor the lane width a pair gets change a
 // score, a coordinate or a string.
 #include <algorithm>
+#include <cstdint>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -134,7 +135,10 @@ int tsq_server::launch(Slot &s, std::vector<std::shared_ptr<Request>> &&reqs, in
       s.pairbuf.push_back(d);
     }
   }
-  if (!s.batch) s.batch.reset(new tsq_batch());
+  if (!s.batch) {
+    s.batch.reset(new tsq_batch());
+    s.batch->async_max = SIZE_MAX;  // growth never waits for the other slots
+  }
   tsq_params p = s.reqs.front()->params;
   if (p.matrix == TSQ_MATRIX_CUSTOM) {
     p.custom_score = s.reqs.front()->custom_score;
