@@ -136,6 +136,14 @@ int tsq_align_pair(const uint8_t *a, int32_t la, const uint8_t *b, int32_t lb,
 void tsq_result_free(tsq_result *r);
 /* Releases the strings of n results. */
 void tsq_results_free(tsq_result *r, int64_t n);
+/* Copies the gapped strings of n results into one caller buffer, for
+ * callers that take all of them at once (a binding that turns them into its
+ * own string objects): for each result with strings, aln_a then aln_b,
+ * n_cols bytes each, no terminators, back to back in result order; results
+ * without strings contribute nothing.  Returns the bytes the strings take;
+ * copies only when buf is not NULL and buf_len is at least that.  Negative
+ * status on bad arguments.  Reads the results only (no device work). */
+int64_t tsq_results_strings(const tsq_result *r, int64_t n, char *buf, int64_t buf_len);
 
 /* ---- Batched form -------------------------------------------------------- */
 

@@ -6,6 +6,7 @@ import os
 import re
 import subprocess
 
+import numpy as np
 import pytest
 
 from tweakseq_gb300 import _native as N
@@ -17,7 +18,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def header_functions():
     text = open(os.path.join(ROOT, "include", "tweakseq_gb300.h")).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return set(re.findall(r"^\s*(?:int|void|size_t)\s+\*?\s*(tsq_\w+)\s*\(", text, flags=re.M))
+    return set(re.findall(r"^\s*(?:int|void|size_t|int64_t)\s+\*?\s*(tsq_\w+)\s*\(", text, flags=re.M))
 
 
 @pytest.fixture(scope="module")
@@ -54,3 +55,31 @@ def test_version_and_struct_layouts(lib):
     assert ctypes.sizeof(N.Result) == 48
     assert ctypes.sizeof(N.PairDesc) == 24
     assert N.TREE_NODE_DTYPE.itemsize == 48
+
+
+def test_results_strings_packs_every_string(lib):
+    """tsq_results_strings reads host results only: aln_a then aln_b of each
+    result with strings, n_cols bytes each, back to back."""
+    texts = [(b"AC-GT", b"ACTG-"), None, (b"", b""), (b"W", b"-")]
+    keep = []
+    raw = np.zeros(len(texts), dtype=N.RESULT_DTYPE)
+    for k, t in enumerate(texts):
+        if t is None:
+            continue
+        a, b = ctypes.create_string_buffer(t[0] + b"\0"), ctypes.create_string_buffer(t[1] + b"\0")
+        keep += [a, b]
+        raw["aln_a"][k], raw["aln_b"][k] = ctypes.addressof(a), ctypes.addressof(b)
+        raw["n_cols"][k] = len(t[0])
+    want = b"AC-GTACTG-" + b"W-"
+    assert lib.tsq_results_strings(raw.ctypes.data, len(raw), None, 0) == len(want)
+    small = ctypes.create_string_buffer(b"x" * 4)
+    assert lib.tsq_results_strings(raw.ctypes.data, len(raw), small, 4) == len(want)
+    assert small.raw[:4] == b"xxxx"  # too small: nothing copied
+    buf = ctypes.create_string_buffer(len(want))
+    assert lib.tsq_results_strings(raw.ctypes.data, len(raw), buf, len(want)) == len(want)
+    assert buf.raw == want
+    assert lib.tsq_results_strings(None, 0, None, 0) == 0
+    assert lib.tsq_results_strings(None, 2, None, 0) == N.E_INVALID_ARG
+    assert lib.tsq_results_strings(raw.ctypes.data, -1, None, 0) == N.E_INVALID_ARG
+    raw["n_cols"][0] = -1
+    assert lib.tsq_results_strings(raw.ctypes.data, len(raw), None, 0) == N.E_INVALID_ARG

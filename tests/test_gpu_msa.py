@@ -56,6 +56,17 @@ def test_consensus_every_byte_class_and_plurality():
             _check_consensus(rows, plur)
 
 
+@pytest.mark.parametrize("first", [0, 31, 32, 33, 64, 99])
+def test_consensus_winner_found_past_the_first_rows(first):
+    """Gaps down to row `first`, then W: W wins every column and its first
+    row is `first` (the warp scans 32 rows per step)."""
+    rows = np.full((100, 40), ord("-"), dtype=np.uint8)
+    rows[first:, :] = ord("W")
+    rows[first:, 7] = ord("C")
+    _check_consensus(rows)
+    _check_consensus(rows, plurality=5.0)
+
+
 def test_consensus_device_entry_point():
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(12)

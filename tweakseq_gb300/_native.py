@@ -128,6 +128,7 @@ _SIGS = {
     "tsq_align_pair": ([_VP, ctypes.c_int32, _VP, ctypes.c_int32, ctypes.POINTER(Params), _VP], ctypes.c_int),
     "tsq_result_free": ([_VP], None),
     "tsq_results_free": ([_VP, ctypes.c_int64], None),
+    "tsq_results_strings": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64], ctypes.c_int64),
     "tsq_align_batch": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.POINTER(Params), ctypes.POINTER(BatchOpts),
                          _VP], ctypes.c_int),
     "tsq_batch_create": ([_VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.POINTER(Params),

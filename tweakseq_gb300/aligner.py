@@ -101,12 +101,23 @@ def _collect(raw: np.ndarray, strings: bool) -> BatchResult:
         table[k] = raw[k]
     sa = sb = None
     if strings:
+        # All strings in one copy (tsq_results_strings), then slices of one
+        # decoded text: a string_at per string costs more than the alignment.
+        ptr = raw.ctypes.data if len(raw) else None
+        total = L.tsq_results_strings(ptr, len(raw), None, 0)
+        N.check(min(total, 0), "tsq_results_strings")
+        buf = np.empty(max(total, 1), dtype=np.uint8)
+        got = L.tsq_results_strings(ptr, len(raw), buf.ctypes.data, total)
+        N.check(min(got, 0), "tsq_results_strings")
+        text = buf[:total].tobytes().decode("ascii")
+        has = ((raw["aln_a"] != 0) & (raw["aln_b"] != 0)).tolist()
+        lens = np.where(has, raw["n_cols"], 0).astype(np.int64)
+        ends = np.cumsum(2 * lens).tolist()
         sa, sb = [], []
-        pa, pb, nc = raw["aln_a"], raw["aln_b"], raw["n_cols"]
-        for k in range(len(raw)):
-            if pa[k]:
-                sa.append(ctypes.string_at(int(pa[k]), int(nc[k])).decode("ascii"))
-                sb.append(ctypes.string_at(int(pb[k]), int(nc[k])).decode("ascii"))
+        for h, c, e in zip(has, lens.tolist(), ends):
+            if h:
+                sa.append(text[e - 2 * c:e - c])
+                sb.append(text[e - c:e])
             else:
                 sa.append(None)
                 sb.append(None)

@@ -285,6 +285,26 @@ void tsq_results_free(tsq_result *r, int64_t n) {
   for (int64_t k = 0; k < n; ++k) tsq_result_free(&r[k]);
 }
 
+int64_t tsq_results_strings(const tsq_result *r, int64_t n, char *buf, int64_t buf_len) {
+  if (n < 0 || (n > 0 && !r) || buf_len < 0) return TSQ_E_INVALID_ARG;
+  int64_t total = 0;
+  for (int64_t k = 0; k < n; ++k) {
+    if (!r[k].aln_a || !r[k].aln_b) continue;
+    if (r[k].n_cols < 0) return TSQ_E_INVALID_ARG;
+    total += 2 * int64_t(r[k].n_cols);
+  }
+  if (!buf || buf_len < total) return total;
+  char *o = buf;
+  for (int64_t k = 0; k < n; ++k) {
+    if (!r[k].aln_a || !r[k].aln_b) continue;
+    const size_t L = size_t(r[k].n_cols);
+    std::memcpy(o, r[k].aln_a, L);
+    std::memcpy(o + L, r[k].aln_b, L);
+    o += 2 * L;
+  }
+  return total;
+}
+
 int tsq_align_pair(const uint8_t *a, int32_t la, const uint8_t *b, int32_t lb, const tsq_params *p,
                    tsq_result *out) {
   return guarded([&]() -> int {

@@ -94,62 +94,71 @@ __global__ void consensus_init_kernel(uint32_t *cnt, int64_t n) {
     cnt[k] = 0u;
 }
 
-// One thread per column: the 24 class sums from the counts, then the first
-// row (in row order) whose class has the highest sum -- the row the
-// reference's loop settles on.  The scan usually ends within a few rows (a
-// winning class is a frequent one); consecutive threads read consecutive
-// columns of a row.
-__global__ void consensus_finish_kernel(const uint8_t *__restrict__ rows, int32_t nseq, int32_t ncols, int64_t stride,
-                                        double plurality, const uint32_t *__restrict__ cnt, uint8_t *out,
-                                        int32_t *best_score, int32_t *best_matches) {
+// One warp per column: lane x < 24 forms class x's sum of pair scores
+// against the column's counts (less the row's own pair) and its count of
+// positive pairs; the warp takes the best sum over the classes present, and
+// then the first row (in row order) whose class holds it -- the row the
+// reference's loop settles on -- scanning 32 rows per ballot.  The scan
+// usually ends in the first ballot (a winning class is a frequent one).
+constexpr int kFinishWarps = 8;
+__global__ void __launch_bounds__(kFinishWarps * 32)
+    consensus_finish_kernel(const uint8_t *__restrict__ rows, int32_t nseq, int32_t ncols, int64_t stride,
+                            double plurality, const uint32_t *__restrict__ cnt, uint8_t *out, int32_t *best_score,
+                            int32_t *best_matches) {
   __shared__ uint8_t cls[256];
+  __shared__ int8_t pair[kClasses][kClasses + 1];
+  __shared__ uint32_t n_s[kFinishWarps][kClasses];
   for (int k = threadIdx.x; k < 256; k += blockDim.x) cls[k] = c_class[k];
+  for (int k = threadIdx.x; k < kClasses * kClasses; k += blockDim.x)
+    pair[k / kClasses][k % kClasses] = c_pair[k / kClasses][k % kClasses];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int32_t col = blockIdx.x * kFinishWarps + w;
+  if (col < ncols && lane < kClasses) n_s[w][lane] = cnt[int64_t(col) * kClasses + lane];
   __syncthreads();
-  const int32_t col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncols) return;
-  int64_t n[kClasses];
-#pragma unroll
-  for (int y = 0; y < kClasses; ++y) n[y] = cnt[int64_t(col) * kClasses + y];
-  int64_t bs = 0;
-  uint32_t winners = 0u;  // classes holding the best sum
-  int64_t score[kClasses], match[kClasses];
-#pragma unroll
-  for (int x = 0; x < kClasses; ++x) {
-    int64_t sx = 0, mt = 0;
-#pragma unroll
-    for (int y = 0; y < kClasses; ++y) {
-      const int v = c_pair[x][y];
-      sx += n[y] * v;
-      if (v > 0) mt += n[y];
-    }
-    // A row does not score against itself.
-    sx -= c_pair[x][x];
-    if (c_pair[x][x] > 0) mt -= 1;
-    score[x] = sx;
-    match[x] = mt;
-    if (n[x] == 0) continue;
-    if (winners == 0u || sx > bs) {
-      bs = sx;
-      winners = 1u << x;
-    } else if (sx == bs) {
-      winners |= 1u << x;
-    }
+  const int x = lane < kClasses ? lane : 0;
+  int64_t sx = 0, mt = 0;
+#pragma unroll 8
+  for (int y = 0; y < kClasses; ++y) {
+    const int64_t ny = n_s[w][y];
+    const int v = pair[x][y];
+    sx += ny * v;
+    if (v > 0) mt += ny;
   }
-  int32_t r = 0;
+  // A row does not score against itself.
+  sx -= pair[x][x];
+  if (pair[x][x] > 0) mt -= 1;
+  const bool present = lane < kClasses && n_s[w][x] != 0u;
+  int64_t bs = present ? sx : INT64_MIN;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const int64_t other = __shfl_xor_sync(0xffffffffu, bs, o);
+    bs = other > bs ? other : bs;
+  }
+  const uint32_t winners = __ballot_sync(0xffffffffu, present && sx == bs);  // classes holding the best sum
+  int32_t r = -1;
   int c = 0;
-  for (; r < nseq; ++r) {
-    c = cls[rows[int64_t(r) * stride + col]];
-    if ((winners >> c) & 1u) break;
+  for (int32_t r0 = 0; r0 < nseq; r0 += 32) {
+    const int32_t rr = r0 + lane;
+    const int cl = rr < nseq ? int(cls[rows[int64_t(rr) * stride + col]]) : 0;
+    const uint32_t hit = __ballot_sync(0xffffffffu, rr < nseq && ((winners >> cl) & 1u));
+    if (hit) {
+      const int first = __ffs(hit) - 1;
+      r = r0 + first;
+      c = __shfl_sync(0xffffffffu, cl, first);
+      break;
+    }
   }
-  if (r >= nseq) r = nseq - 1;  // a winning class always occurs; stays in bounds regardless
-  int64_t bm = 0;
-#pragma unroll
-  for (int x = 0; x < kClasses; ++x)
-    if (x == c) bm = match[x];
-  (void)score;
-  out[col] = double(bm) >= plurality ? rows[int64_t(r) * stride + col] : uint8_t('?');
-  if (best_score) best_score[col] = int32_t(bs);
-  if (best_matches) best_matches[col] = int32_t(bm);
+  if (r < 0) {  // (a winning class always occurs; stays in bounds regardless)
+    r = nseq - 1;
+    c = cls[rows[int64_t(r) * stride + col]];
+  }
+  const int64_t bm = __shfl_sync(0xffffffffu, mt, c);
+  if (lane == 0) {
+    out[col] = double(bm) >= plurality ? rows[int64_t(r) * stride + col] : uint8_t('?');
+    if (best_score) best_score[col] = int32_t(bs);
+    if (best_matches) best_matches[col] = int32_t(bm);
+  }
 }
 
 // BLOSUM62 row of each letter 'A'..'Z' (J, O, U, X share the X row), as the
@@ -222,8 +231,8 @@ cudaError_t consensus_enqueue(const uint8_t *d_rows, int32_t nseq, int32_t ncols
   else
     consensus_count_kernel<false><<<dim3(col_tiles, slices), kCountThreads, 0, stream>>>(d_rows, nseq, ncols, stride,
                                                                                        per, cnt);
-  consensus_finish_kernel<<<(ncols + 127) / 128, 128, 0, stream>>>(d_rows, nseq, ncols, stride, plurality, cnt, d_out,
-                                                                   d_score, d_matches);
+  consensus_finish_kernel<<<(ncols + kFinishWarps - 1) / kFinishWarps, kFinishWarps * 32, 0, stream>>>(
+      d_rows, nseq, ncols, stride, plurality, cnt, d_out, d_score, d_matches);
   return cudaGetLastError();
 }
 

@@ -119,7 +119,7 @@ void build_lut(const Scheme &s, uint8_t lut[256]);
 // Byte -> score class (kBadCode for bytes the scheme rejects).
 void build_class_lut(const Scheme &s, uint8_t lut[256]);
 
-// Kernel launchers (fill_kernels.cu, walk_kernel.cu, encode in batch.cu).
+// Kernel launchers (fill_dispatch.cu, fill_i16.cu, fill_cta.cu, walk_kernel.cu).
 // Returns the number of thread blocks a persistent launch of this shape uses.
 // A launch covers every lane width G of one row height R and lane type
 // (i16: 0 int32, 1 int16x2, 2 int16x2 with overflow check).

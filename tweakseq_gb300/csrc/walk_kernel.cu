@@ -15,104 +15,20 @@
 namespace tsq {
 namespace {
 
-constexpr int kWalkThreads = 128;
-constexpr int kWin = 16;  // steps per plane window
-
-// Direction nibbles of one pair, read through a window: the words of steps
-// ws-15..ws for lanes wt-1 and wt of one band, loaded together into this
-// thread's shared-memory slots.  A walk moves one step left or one row up
-// at a time, so most nibbles come from the window and the window's 32 loads
-// are independent of each other (one global-memory latency per refill
-// instead of one per step).  Row i is tracked as (band, lane t, row r).
-struct PlaneWalk {
-  const uint32_t *words;  // planes as 32-bit entries: 8 rows x 4 bits
-  uint32_t *win;          // 2 * kWin shared words of this thread
-  int n, G, P;
-  int band, t, r;                       // position of row i (1-based i >= 1)
-  int wband = -1, wt = -1, ws = -1;     // the window
-  __device__ void set_row(int i) {
-    const int row0 = i - 1;
-    band = row0 / P;
-    const int w = row0 - band * P;
-    t = w >> 3;
-    r = w & 7;
-  }
-  __device__ void up() {  // i -> i - 1
-    if (--r < 0) {
-      r = 7;
-      if (--t < 0) {
-        t = G - 1;
-        --band;
-      }
-    }
-  }
-  __device__ void refill(int s) {
-    wband = band;
-    wt = t;
-    ws = s;
-    const int64_t row = (int64_t)band * (n + G - 1);
-    // All loads first (addresses clamped into the band, unused slots read a
-    // valid word), then the stores: the loads overlap instead of each
-    // waiting for the previous store.
-    uint32_t v[2 * kWin];
-#pragma unroll
-    for (int k = 0; k < kWin; ++k) {
-      const int64_t e = (row + max(s - k, 0)) * G + t;
-      v[2 * k + 1] = __ldg(words + e);
-      v[2 * k] = __ldg(words + (t > 0 ? e - 1 : e));
-    }
-#pragma unroll
-    for (int k = 0; k < 2 * kWin; ++k) win[k] = v[k];
-  }
-  // Nibble of cell (i, j), i the current row, j >= 1.
-  __device__ int nib(int j) {
-    const int s = j - 1 + t;
-    if (band != wband || (t != wt && t != wt - 1) || s > ws || s <= ws - kWin) refill(s);
-    const uint32_t w = win[2 * (ws - s) + (t == wt ? 1 : 0)];
-    return int(w >> (4 * r)) & 15;
-  }
-};
-
-// One sequence read backwards through a 16-byte window.
-struct SeqWalk {
-  const uint8_t *base;
-  uintptr_t blk = ~uintptr_t(0);
-  uint4 v;
-  __device__ uint8_t at(int idx) {
-    const uintptr_t addr = reinterpret_cast<uintptr_t>(base) + uintptr_t(idx);
-    const uintptr_t b = addr & ~uintptr_t(15);
-    if (b != blk) {
-      v = *reinterpret_cast<const uint4 *>(b);
-      blk = b;
-    }
-    const int o = int(addr - b);
-    const uint32_t w = o < 8 ? (o < 4 ? v.x : v.y) : (o < 12 ? v.z : v.w);
-    return uint8_t(w >> (8 * (o & 3)));
-  }
-};
-
-__global__ void __launch_bounds__(kWalkThreads) walk_kernel(const WalkArgs A) {
-  __shared__ uint32_t s_win[kWalkThreads * 2 * kWin];
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= A.n_tasks) return;
-  const int p = A.tasks[k];
-  const PairDev pr = A.pairs[p];
-  ResultDev &res = A.res[p];
-  if (res.status != TSQ_OK) return;
+// The walk of one pair, from its end cell back to its start, through a
+// plane reader and two sequence readers.  Every lane of the pair's warp runs
+// it with the same values (warp-uniform branches); only `writer` stores.
+template <class Plane, class Seq>
+__device__ __forceinline__ void walk_pair(const WalkArgs &A, const PairDev &pr, ResultDev &res, Plane &pl, Seq &a,
+                                          Seq &b, char *out_a, char *out_b, int64_t cap, bool writer) {
   const int m = pr.a_len, n = pr.b_len;
-  SeqWalk a{A.seqs + pr.a_off}, b{A.seqs + pr.b_off};
-  const int64_t cap = (int64_t)m + n;
-  char *out_a = A.aln + A.aln_off[p];
-  char *out_b = out_a + cap;
-  const int G = A.shape_G[p];
-  PlaneWalk pl{reinterpret_cast<const uint32_t *>(A.planes + A.plane_off[p]), s_win + threadIdx.x * 2 * kWin, n, G,
-               G * A.shape_R[p]};
-
   int i, j;
   if (A.local) {
     if (res.score <= 0) {
-      res.a_begin = res.a_end = res.b_begin = res.b_end = 0;
-      res.n_ident = res.n_cols = 0;
+      if (writer) {
+        res.a_begin = res.a_end = res.b_begin = res.b_end = 0;
+        res.n_ident = res.n_cols = 0;
+      }
       return;
     }
     i = res.a_end;
@@ -127,7 +43,7 @@ __global__ void __launch_bounds__(kWalkThreads) walk_kernel(const WalkArgs A) {
   int ident = 0;
   for (;;) {
     if (L >= cap && (i > 0 || j > 0)) {  // cannot happen with valid planes
-      res.status = TSQ_E_CUDA;
+      if (writer) res.status = TSQ_E_CUDA;
       return;
     }
     if (state == 0) {
@@ -138,15 +54,21 @@ __global__ void __launch_bounds__(kWalkThreads) walk_kernel(const WalkArgs A) {
       }
       if (i == 0) {  // global top row: one horizontal gap run
         ++L;
-        out_a[cap - L] = '-';
-        out_b[cap - L] = char(b.at(j - 1));
+        const char cb = char(b.at(j - 1));
+        if (writer) {
+          out_a[cap - L] = '-';
+          out_b[cap - L] = cb;
+        }
         --j;
         continue;
       }
       if (j == 0) {  // global left column: one vertical gap run
         ++L;
-        out_a[cap - L] = char(a.at(i - 1));
-        out_b[cap - L] = '-';
+        const char ca = char(a.at(i - 1));
+        if (writer) {
+          out_a[cap - L] = ca;
+          out_b[cap - L] = '-';
+        }
         --i;
         if (i > 0) pl.up();
         continue;
@@ -155,8 +77,10 @@ __global__ void __launch_bounds__(kWalkThreads) walk_kernel(const WalkArgs A) {
       if (hd == kDirDiag) {
         ++L;
         const uint8_t ca = a.at(i - 1), cb = b.at(j - 1);
-        out_a[cap - L] = char(ca);
-        out_b[cap - L] = char(cb);
+        if (writer) {
+          out_a[cap - L] = char(ca);
+          out_b[cap - L] = char(cb);
+        }
         ident += ca == cb;
         --i;
         --j;
@@ -168,29 +92,36 @@ __global__ void __launch_bounds__(kWalkThreads) walk_kernel(const WalkArgs A) {
       // An E run always ends inside the matrix (E(i,0) is minus infinity);
       // if the planes say otherwise, stop instead of leaving the matrix.
       if (j <= 0 || i <= 0) {
-        res.status = TSQ_E_CUDA;
+        if (writer) res.status = TSQ_E_CUDA;
         return;
       }
       const int d = pl.nib(j);
       ++L;
-      out_a[cap - L] = '-';
-      out_b[cap - L] = char(b.at(j - 1));
+      const char cb = char(b.at(j - 1));
+      if (writer) {
+        out_a[cap - L] = '-';
+        out_b[cap - L] = cb;
+      }
       --j;
       if (d & 4) state = 0;
     } else {
       if (i <= 0 || j <= 0) {
-        res.status = TSQ_E_CUDA;
+        if (writer) res.status = TSQ_E_CUDA;
         return;
       }
       const int d = pl.nib(j);
       ++L;
-      out_a[cap - L] = char(a.at(i - 1));
-      out_b[cap - L] = '-';
+      const char ca = char(a.at(i - 1));
+      if (writer) {
+        out_a[cap - L] = ca;
+        out_b[cap - L] = '-';
+      }
       --i;
       if (i > 0) pl.up();
       if (d & 8) state = 0;
     }
   }
+  if (!writer) return;
   res.a_begin = i;
   res.b_begin = j;
   if (!A.local) {
@@ -199,6 +130,107 @@ __global__ void __launch_bounds__(kWalkThreads) walk_kernel(const WalkArgs A) {
   }
   res.n_cols = int32_t(L);
   res.n_ident = ident;
+}
+
+// One warp per pair, every lane running the pair's walk with the same
+// values, so a window refill costs the warp one coalesced load per lane and
+// the warp waits only for its own pair's refills.  (A thread per pair made
+// each warp wait for all 32 of its pairs' refills in turn: 0.77 against
+// 0.14 ms on 2,016 protein pairs, 18.3 against 3.2 ms on 32 long DNA pairs,
+// 3.8 against 3.6 ms on 100,000 pairs.)
+constexpr int kWarpWalkWarps = 4;
+constexpr int kWS = 32, kWL = 4;  // plane window: 32 steps x 4 lanes of one band
+constexpr int kSeqWin = 128;      // residues per sequence window
+
+struct WarpPlane {
+  const uint32_t *words;
+  uint32_t *win;  // kWS * kWL words of this warp
+  int n, G, P, lane;
+  int band, t, r;
+  int wband = -1, wt = -1, ws = -1;
+  __device__ void set_row(int i) {
+    const int row0 = i - 1;
+    band = row0 / P;
+    const int w = row0 - band * P;
+    t = w >> 3;
+    r = w & 7;
+  }
+  __device__ void up() {
+    if (--r < 0) {
+      r = 7;
+      if (--t < 0) {
+        t = G - 1;
+        --band;
+      }
+    }
+  }
+  // Steps s-kWS+1..s of lanes t-kWL+1..t (clamped into the band).
+  __device__ void refill(int s) {
+    wband = band;
+    wt = t;
+    ws = s;
+    const int64_t row = (int64_t)band * (n + G - 1);
+    uint32_t v[kWS * kWL / 32];
+#pragma unroll
+    for (int q = 0; q < kWS * kWL / 32; ++q) {
+      const int w = lane + 32 * q;
+      const int ss = max(s - w / kWL, 0), tt = max(t - w % kWL, 0);
+      v[q] = __ldg(words + (row + ss) * G + tt);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < kWS * kWL / 32; ++q) win[lane + 32 * q] = v[q];
+    __syncwarp();
+  }
+  __device__ int nib(int j) {
+    const int s = j - 1 + t;
+    if (band != wband || t > wt || t <= wt - kWL || s > ws || s <= ws - kWS) refill(s);
+    return int(win[(ws - s) * kWL + (wt - t)] >> (4 * r)) & 15;
+  }
+};
+
+// One sequence read backwards through a shared window of kSeqWin residues.
+struct WarpSeq {
+  const uint8_t *base;
+  int len;
+  uint8_t *win;
+  int lane;
+  int lo = 1 << 30;
+  __device__ uint8_t at(int idx) {
+    if (idx < lo || idx >= lo + kSeqWin) {
+      lo = max(0, idx - kSeqWin + 1);
+      uint8_t v[kSeqWin / 32];
+#pragma unroll
+      for (int q = 0; q < kSeqWin / 32; ++q) {
+        const int k = lo + lane + 32 * q;
+        v[q] = k < len ? base[k] : uint8_t(0);
+      }
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < kSeqWin / 32; ++q) win[lane + 32 * q] = v[q];
+      __syncwarp();
+    }
+    return win[idx - lo];
+  }
+};
+
+__global__ void __launch_bounds__(kWarpWalkWarps * 32) walk_warp_kernel(const WalkArgs A) {
+  __shared__ uint32_t s_plane[kWarpWalkWarps][kWS * kWL];
+  __shared__ uint8_t s_seq[kWarpWalkWarps][2][kSeqWin];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int k = blockIdx.x * kWarpWalkWarps + w;
+  if (k >= A.n_tasks) return;
+  const int p = A.tasks[k];
+  const PairDev pr = A.pairs[p];
+  ResultDev &res = A.res[p];
+  if (res.status != TSQ_OK) return;
+  WarpSeq a{A.seqs + pr.a_off, pr.a_len, s_seq[w][0], lane}, b{A.seqs + pr.b_off, pr.b_len, s_seq[w][1], lane};
+  const int64_t cap = (int64_t)pr.a_len + pr.b_len;
+  char *out_a = A.aln + A.aln_off[p];
+  const int G = A.shape_G[p];
+  WarpPlane pl{reinterpret_cast<const uint32_t *>(A.planes + A.plane_off[p]), s_plane[w], pr.b_len, G,
+               G * A.shape_R[p], lane};
+  walk_pair(A, pr, res, pl, a, b, out_a, out_a + cap, cap, lane == 0);
 }
 
 // ASCII -> letter codes, and (when clut is set) -> score classes for the
@@ -243,8 +275,8 @@ __global__ void encode_kernel(const uint8_t *__restrict__ seqs, int64_t len, con
 
 cudaError_t launch_walk(const WalkArgs &a, cudaStream_t st) {
   if (a.n_tasks <= 0) return cudaSuccess;
-  const int blocks = (a.n_tasks + kWalkThreads - 1) / kWalkThreads;
-  walk_kernel<<<blocks, kWalkThreads, 0, st>>>(a);
+  const int blocks = (a.n_tasks + kWarpWalkWarps - 1) / kWarpWalkWarps;
+  walk_warp_kernel<<<blocks, kWarpWalkWarps * 32, 0, st>>>(a);
   return cudaGetLastError();
 }
 
