@@ -9,12 +9,13 @@
 // the plurality (default nseq / 2, :163-172), else '?'.
 //
 // A row's sum depends only on its class (23 BLOSUM62 rows + the gap class),
-// so the kernel counts classes per column (one pass over the bytes,
-// HBM-bound), and the finishing kernel evaluates the 24 class sums from the
-// counts: score(x) = sum_y count(y) S(x,y) - S(x,x), then scans the column
-// from the first row for the first row whose class holds the best sum.  All
-// terms are integers, so this equals the reference's double sums exactly,
-// and the row found is the first row with the best score, as there.
+// so the kernel counts bytes per column in 27 bins ('A'..'Z' and everything
+// else; one pass over the bytes), and the finishing kernel folds the bins
+// into the 24 classes, evaluates the class sums from the counts:
+// score(x) = sum_y count(y) S(x,y) - S(x,x), then scans the column from the
+// first row for the first row whose class holds the best sum.  All terms are
+// integers, so this equals the reference's double sums exactly, and the row
+// found is the first row with the best score, as there.
 #include <climits>
 #include <cstring>
 
@@ -25,30 +26,42 @@ namespace {
 
 constexpr int kClasses = 24;  // BLOSUM62 rows 0..22, 23 = gap class
 constexpr int kGapClass = 23;
+constexpr int kBins = 27;  // counted per column: 'A'..'Z', then every other byte
+constexpr int kOtherBin = 26;
 constexpr int kCountWarps = 8;
 constexpr int kCountThreads = kCountWarps * 32;
 constexpr int kTile = 128;  // columns per block
 
 __constant__ int8_t c_pair[kClasses][kClasses];  // class-vs-class pair scores
 __constant__ uint8_t c_class[256];                // byte -> class
+__constant__ uint8_t c_bin_class[kBins];          // counting bin -> class
+
+// Counting bin of each byte of a word, four at a time: 'A'..'Z' -> 0..25,
+// every other byte -> 26 (per-byte SIMD subtract and compare).
+__device__ __forceinline__ uint32_t bins4(uint32_t v) {
+  const uint32_t d = __vsub4(v, 0x41414141u);
+  const uint32_t lt = __vcmpltu4(d, 0x1a1a1a1au);  // 0xff in the letter bytes
+  return (d & lt) | (0x1a1a1a1au & ~lt);
+}
 
 // A block covers 128 columns (lane t holds columns t, t+32, t+64, t+96 of
 // the tile, so that its counters fall in bank t) and one slice of the rows,
 // striped over its 8 warps.  With 4-byte-aligned rows a lane reads its 4
-// columns of a row with one 32-bit load, eight rows' loads in flight.  The
-// counts go to one shared histogram per block (shared-memory atomics), then
-// into the column totals with global atomics.  Only counts: the first row of
-// a class is needed for the winning classes alone and is found afterwards.
+// columns of a row with one 32-bit load, eight rows' loads in flight, bins
+// the four bytes with two SIMD instructions and adds each to its column's
+// bin with one shared-memory atomic -- the one shared-memory operation per
+// byte, which sets the pace.  The counts go to one shared histogram per
+// block, then into the column totals with global atomics.  Only counts: the
+// first row of a class is needed for the winning classes alone and is found
+// afterwards.
 template <bool kVec>
 __global__ void __launch_bounds__(kCountThreads) consensus_count_kernel(const uint8_t *__restrict__ rows, int32_t nseq,
                                                                         int32_t ncols, int64_t stride,
                                                                         int32_t rows_per_slice, uint32_t *cnt) {
-  __shared__ uint32_t h[kClasses][kTile];
-  __shared__ uint8_t cls[256];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int k = threadIdx.x; k < kClasses * kTile; k += kCountThreads) (&h[0][0])[k] = 0u;
-  for (int k = threadIdx.x; k < 256; k += kCountThreads) cls[k] = c_class[k];
+  __shared__ uint32_t h[kBins][kTile];
+  for (int k = threadIdx.x; k < kBins * kTile; k += kCountThreads) (&h[0][0])[k] = 0u;
   __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t c0 = blockIdx.x * kTile;
   const int32_t r0 = blockIdx.y * rows_per_slice;
   const int32_t r1 = min(nseq, r0 + rows_per_slice);
@@ -57,35 +70,44 @@ __global__ void __launch_bounds__(kCountThreads) consensus_count_kernel(const ui
   const int nvalid = max(0, min(4, ncols - mc));
   if (nvalid > 0) {
     const uint8_t *p = rows + mc;
-    auto load = [&](int32_t r) -> uint32_t {
-      if (kVec && nvalid == 4) return __ldg(reinterpret_cast<const uint32_t *>(p + int64_t(r) * stride));
-      uint32_t v = 0;
-      for (int u = 0; u < nvalid; ++u) v |= uint32_t(__ldg(p + int64_t(r) * stride + u)) << (8 * u);
-      return v;
-    };
-    auto count = [&](uint32_t v) {
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (u < nvalid) atomicAdd(&h[cls[(v >> (8 * u)) & 0xffu]][lane + 32 * u], 1u);
-    };
+    uint32_t *hb = &h[0][lane];
     constexpr int kRows = 8;
     int32_t r = r0 + w;
-    for (; r + (kRows - 1) * kCountWarps < r1; r += kRows * kCountWarps) {
-      uint32_t v[kRows];
+    if (kVec && nvalid == 4) {
+      auto count4 = [&](uint32_t v) {
+        const uint32_t b = bins4(v);
+        atomicAdd(hb + __byte_perm(b, 0u, 0x4440u) * kTile, 1u);
+        atomicAdd(hb + 32 + __byte_perm(b, 0u, 0x4441u) * kTile, 1u);
+        atomicAdd(hb + 64 + __byte_perm(b, 0u, 0x4442u) * kTile, 1u);
+        atomicAdd(hb + 96 + __byte_perm(b, 0u, 0x4443u) * kTile, 1u);
+      };
+      const uint32_t *pw = reinterpret_cast<const uint32_t *>(p);
+      const int64_t wstride = stride / 4;
+      for (; r + (kRows - 1) * kCountWarps < r1; r += kRows * kCountWarps) {
+        uint32_t v[kRows];
 #pragma unroll
-      for (int q = 0; q < kRows; ++q) v[q] = load(r + q * kCountWarps);
+        for (int q = 0; q < kRows; ++q) v[q] = __ldg(pw + int64_t(r + q * kCountWarps) * wstride);
 #pragma unroll
-      for (int q = 0; q < kRows; ++q) count(v[q]);
+        for (int q = 0; q < kRows; ++q) count4(v[q]);
+      }
+      for (; r < r1; r += kCountWarps) count4(__ldg(pw + int64_t(r) * wstride));
+    } else {
+      // Ragged last columns or unaligned rows: byte loads.
+      for (; r < r1; r += kCountWarps) {
+        uint32_t v = 0;
+        for (int u = 0; u < nvalid; ++u) v |= uint32_t(__ldg(p + int64_t(r) * stride + u)) << (8 * u);
+        const uint32_t b = bins4(v);
+        for (int u = 0; u < nvalid; ++u) atomicAdd(hb + 32 * u + ((b >> (8 * u)) & 0xffu) * kTile, 1u);
+      }
     }
-    for (; r < r1; r += kCountWarps) count(load(r));
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < kClasses * kTile; e += kCountThreads) {
-    const int c = e / kTile, slot = e % kTile;
-    const uint32_t s = h[c][slot];
+  for (int e = threadIdx.x; e < kBins * kTile; e += kCountThreads) {
+    const int bin = e / kTile, slot = e % kTile;
+    const uint32_t s = h[bin][slot];
     // Tile slot lane + 32u holds memory column c0 + 4*lane + u.
     const int32_t col = c0 + 4 * (slot & 31) + (slot >> 5);
-    if (s != 0u && col < ncols) atomicAdd(&cnt[int64_t(col) * kClasses + c], s);
+    if (s != 0u && col < ncols) atomicAdd(&cnt[int64_t(col) * kBins + bin], s);
   }
 }
 
@@ -113,7 +135,14 @@ __global__ void __launch_bounds__(kFinishWarps * 32)
     pair[k / kClasses][k % kClasses] = c_pair[k / kClasses][k % kClasses];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t col = blockIdx.x * kFinishWarps + w;
-  if (col < ncols && lane < kClasses) n_s[w][lane] = cnt[int64_t(col) * kClasses + lane];
+  __shared__ uint32_t bin_s[kFinishWarps][kBins];
+  if (col < ncols && lane < kBins) bin_s[w][lane] = cnt[int64_t(col) * kBins + lane];
+  __syncwarp();
+  if (col < ncols && lane < kClasses) {  // fold the bins into the classes
+    uint32_t c = 0u;
+    for (int b = 0; b < kBins; ++b) c += c_bin_class[b] == lane ? bin_s[w][b] : 0u;
+    n_s[w][lane] = c;
+  }
   __syncthreads();
   if (col >= ncols) return;
   const int x = lane < kClasses ? lane : 0;
@@ -163,12 +192,14 @@ __global__ void __launch_bounds__(kFinishWarps * 32)
 
 // BLOSUM62 row of each letter 'A'..'Z' (J, O, U, X share the X row), as the
 // reference's letter map; everything else is the gap class.
-void class_tables(int8_t pair[kClasses][kClasses], uint8_t cls[256]) {
+void class_tables(int8_t pair[kClasses][kClasses], uint8_t cls[256], uint8_t bin_class[kBins]) {
   static const char kOrder[23] = {'A', 'R', 'N', 'D', 'C', 'Q', 'E', 'G', 'H', 'I', 'L', 'K',
                                   'M', 'F', 'P', 'S', 'T', 'W', 'Y', 'V', 'B', 'Z', 'X'};
   for (int b = 0; b < 256; ++b) cls[b] = kGapClass;
   for (int k = 0; k < 23; ++k) cls[uint8_t(kOrder[k])] = uint8_t(k);
   cls[uint8_t('J')] = cls[uint8_t('O')] = cls[uint8_t('U')] = 22;
+  for (int b = 0; b < 26; ++b) bin_class[b] = cls[uint8_t('A' + b)];
+  bin_class[kOtherBin] = kGapClass;
   for (int x = 0; x < kClasses; ++x)
     for (int y = 0; y < kClasses; ++y) {
       if (x == kGapClass && y == kGapClass)
@@ -187,10 +218,11 @@ cudaError_t upload_tables() {
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || done_dev == dev) return e;
   int8_t pair[kClasses][kClasses];
-  uint8_t cls[256];
-  class_tables(pair, cls);
+  uint8_t cls[256], bin_class[kBins];
+  class_tables(pair, cls, bin_class);
   e = cudaMemcpyToSymbol(c_pair, pair, sizeof(pair));
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_class, cls, sizeof(cls));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_bin_class, bin_class, sizeof(bin_class));
   if (e == cudaSuccess) done_dev = dev;
   return e;
 }
@@ -214,7 +246,7 @@ cudaError_t consensus_enqueue(const uint8_t *d_rows, int32_t nseq, int32_t ncols
   cudaError_t e = upload_tables();
   if (e != cudaSuccess) return e;
   uint32_t *cnt = static_cast<uint32_t *>(scratch);
-  const int64_t entries = int64_t(ncols) * kClasses;
+  const int64_t entries = int64_t(ncols) * kBins;
   consensus_init_kernel<<<int(std::min<int64_t>((entries + 255) / 256, 4096)), 256, 0, stream>>>(cnt, entries);
   // Enough blocks for every SM several times over: split the rows into
   // slices when the columns alone do not give them.
@@ -247,7 +279,7 @@ struct ConsensusCache {
 
 }  // namespace
 
-size_t consensus_scratch_bytes(int32_t ncols) { return size_t(ncols > 0 ? ncols : 0) * kClasses * 4; }
+size_t consensus_scratch_bytes(int32_t ncols) { return size_t(ncols > 0 ? ncols : 0) * kBins * 4; }
 
 }  // namespace tsq
 
