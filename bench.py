@@ -27,6 +27,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import datetime
 import json
 import os
 import re
@@ -75,19 +76,20 @@ def rank_info():
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.proc = None
-        self.lines = []
+        self.lines = []  # (sample wall-clock time, fields)
+        self.window = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                          "-lms", "50", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                          "-lms", "20", "-i", str(self.gpu)], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -96,8 +98,27 @@ class ClockSampler:
         return self
 
     def _read(self):
+        # nvidia-smi's output reaches the pipe in bursts, so each sample is
+        # placed by its own timestamp, not by when it arrives.
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            f = [x.strip() for x in line.split(",")]
+            try:
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except (ValueError, IndexError):
+                continue
+            self.lines.append((ts, f[1:]))
+
+    def wait_started(self, timeout_s=5.0):
+        """Blocks until nvidia-smi has printed its first sample (it takes a
+        while to start), so the samples cover the region timed next."""
+        t_end = time.perf_counter() + timeout_s
+        while self.proc and not self.lines and time.perf_counter() < t_end:
+            time.sleep(0.01)
+
+    def mark(self, t0, t1):
+        """The timed region (wall-clock seconds): only samples taken in it
+        (give or take one sampling period) are summarised."""
+        self.window = (t0 - 0.025, t1 + 0.025)
 
     def __exit__(self, *exc):
         if self.proc:
@@ -110,8 +131,12 @@ class ClockSampler:
     def summary(self):
         sms, maxs, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            f = [x.strip() for x in ln.split(",")]
+        lines = self.lines
+        if self.window:
+            inside = [x for x in lines if self.window[0] <= x[0] <= self.window[1]]
+            # A region shorter than the sampling period: the sample nearest it.
+            lines = inside or sorted(lines, key=lambda x: abs(x[0] - self.window[0]))[:1]
+        for _, f in lines:
             if len(f) < 9:
                 continue
             try:
@@ -216,6 +241,9 @@ def run_ours(args):
     step_ms, fill_ms = [], []
     barrier()
     with ClockSampler(local) as clk:
+        clk.wait_started()
+        barrier()
+        t_region = time.time()
         for _ in range(args.steps):
             with torch.cuda.stream(ext):
                 flush.zero_()
@@ -228,6 +256,7 @@ def run_ours(args):
             step_ms.append(e0.elapsed_time(e1))
             fill_ms.append(batch.stats()["fill_ms"])
         barrier()
+        clk.mark(t_region, time.time())
     from tweakseq_gb300.multi import max_over_ranks
     total_ms = max_over_ranks(float(np.sum(step_ms)))  # the job's time is its slowest rank's
     value = world * cells * args.steps / (total_ms * 1e-3) / 1e9
