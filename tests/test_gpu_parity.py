@@ -359,36 +359,44 @@ def test_chunked_call_equals_single_plan(output, local):
         assert np.array_equal(got.table["b_end"][idx], o["b_end"])
 
 
-def _call_batch(seqs_ptr, seqs_len, tab, output="score"):
+def _call_batch(seqs_ptr, seqs_len, tab, output="score", mode="global"):
     raw = np.zeros(len(tab), dtype=N.RESULT_DTYPE)
-    p, keep = N.make_params(output=output)
+    p, keep = N.make_params(output=output, mode=mode)
     rc = N.lib().tsq_align_batch(seqs_ptr, seqs_len, tab.ctypes.data, len(tab), ctypes.byref(p),
                                  ctypes.byref(A._opts()), raw.ctypes.data)
     return rc, raw
 
 
-@pytest.mark.parametrize("output", ["score", "identity"])
-def test_chunked_call_page_locked_input(output):
-    """Page-locked residues go up whole while the first chunk is planned;
-    the results equal those of the same call on pageable memory, including
-    a pair with an invalid residue in the last chunk."""
+@pytest.mark.parametrize("output,mode", [("score", "global"), ("identity", "global"), ("score", "local")])
+def test_chunked_call_page_locked_input(output, mode):
+    """Page-locked residues are encoded in place and the chunks are cut by
+    cost; the results equal those of the same call on pageable memory
+    (chunks of consecutive pairs), including empty pairs and a pair with an
+    invalid residue, and a sample equals the oracle."""
     torch = pytest.importorskip("torch")
     ps = W.uneven_pairs(n_pairs=40000, seed=14)
     seqs, tab = A._as_inputs(ps)
-    seqs = seqs.copy()
-    seqs[int(tab["a_off"][35000]) + 3] = ord("#")  # pair 35000 is in the last chunk
+    seqs, tab = seqs.copy(), tab.copy()
+    seqs[int(tab["a_off"][35000]) + 3] = ord("#")
+    tab["a_len"][100] = 0
+    tab["b_len"][20000] = 0
     pinned = torch.from_numpy(seqs).pin_memory()
-    rc_p, got = _call_batch(pinned.data_ptr(), len(seqs), tab, output)
-    rc_h, want = _call_batch(seqs.ctypes.data, len(seqs), tab, output)
+    rc_p, got = _call_batch(pinned.data_ptr(), len(seqs), tab, output, mode)
+    rc_h, want = _call_batch(seqs.ctypes.data, len(seqs), tab, output, mode)
     assert rc_p == rc_h == N.E_INVALID_RESIDUE
     assert got["status"][35000] == N.E_INVALID_RESIDUE
-    for f in ("score", "n_ident", "n_cols", "status"):
+    for f in ("score", "a_begin", "a_end", "b_begin", "b_end", "n_ident", "n_cols", "status"):
         assert np.array_equal(got[f], want[f]), f
+    idx = np.random.default_rng(7).choice(len(tab), 200, replace=False)
+    idx = idx[idx != 35000]
+    o = O.batch(seqs, tab["a_off"][idx], tab["a_len"][idx], tab["b_off"][idx], tab["b_len"][idx], O.BLOSUM62, 11, 1,
+                mode == "local", O.MODE_IDENT if output == "identity" else O.MODE_SCORE)
+    assert np.array_equal(got["score"][idx], o["score"])
     bad = tab.copy()
     bad["b_len"][39000] = -1
-    rc, _ = _call_batch(pinned.data_ptr(), len(seqs), bad, output)
+    rc, _ = _call_batch(pinned.data_ptr(), len(seqs), bad, output, mode)
     assert rc == N.E_INVALID_ARG
-    rc, again = _call_batch(pinned.data_ptr(), len(seqs), tab, output)
+    rc, again = _call_batch(pinned.data_ptr(), len(seqs), tab, output, mode)
     assert rc == N.E_INVALID_RESIDUE and np.array_equal(again["score"], want["score"])
 
 
