@@ -161,9 +161,13 @@ __device__ __forceinline__ void stage_chunk_rt(int G, int k, int t, int nact, co
     if (q < kTopCopies) {
       const int e = c0 + q * kPer;
       cp_async16(top_ring + (e & (kTopRing - 1)), top_g + e);
+      // The first 16 bytes of each ring are mirrored past its end (into the
+      // ring's padding), so a read at index + 1 needs no wrap.
+      if ((e & (kTopRing - 1)) == 0) cp_async16(top_ring + kTopRing, top_g + e);
     } else {
       const int64_t a = a0 + 16 * (q - kTopCopies);
       cp_async16(code_ring + (a & (CODE_RING - 1)), codes + a);
+      if ((a & (CODE_RING - 1)) == 0) cp_async16(code_ring + CODE_RING, codes + a);
     }
   }
 }

@@ -239,7 +239,11 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
     const int i0 = min(2 * G, steps_pad);
     const int i1 = max(i0, n_min & ~1);
 
-    auto step = [&](const int s, auto k_tag, auto interior_tag) {
+    // Ring indexes of a step pair: the odd step reads one entry further,
+    // into the mirrored head past the ring's end when the even one is last.
+    const int cA0 = int(boff & (kCodeRing16 - 1)) - t + 1 + kCodeRing16;  // code of column jA + 1, positive
+    const int cB0 = cA0 - G;                                               // code of column jB + 1
+    auto step = [&](const int s, auto k_tag, auto interior_tag, const int ia, const int ib, const int it) {
       constexpr int k = decltype(k_tag)::value;
       constexpr bool INTERIOR = decltype(interior_tag)::value;
       // Chunk boundaries fall on odd steps only (pairs start on even steps).
@@ -255,8 +259,8 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       const int jA = s - t, jB = jA - G;
       const uint2 wa = pa[k], wb = pb[k];
       {
-        const int ca = min(int(code_ring[(boff + jA + 1) & (kCodeRing16 - 1)]), ncls - 1);
-        const int cb = min(int(code_ring[(boff + jB + 1) & (kCodeRing16 - 1)]), ncls - 1);
+        const int ca = min(int(code_ring[ia]), ncls - 1);
+        const int cb = min(int(code_ring[ib]), ncls - 1);
         pa[k ^ 1] = profA[(2 * ca) * kThreads16];
         pb[k ^ 1] = profB[(2 * cb) * kThreads16];
       }
@@ -266,7 +270,7 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       // reads lane 0's ring entry (one broadcast address per group).
       const uint32_t upH = prmt(tv[k], rH, selH);
       const uint32_t upF = prmt(tv[k], rF, selF);
-      tv[k ^ 1] = top_ring[(s + 1) & (kTopRing - 1)];
+      tv[k ^ 1] = top_ring[it];
       const bool vA = INTERIOR || (unsigned)jA < (unsigned)nact;
       const bool vB = INTERIOR || (unsigned)jB < (unsigned)nact;
       if (vA || vB) {
@@ -324,18 +328,15 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       }
     };
     int s0 = 0;
-    for (; s0 < i0; s0 += 2) {
-      step(s0, IntTag<0>{}, BoolTag<false>{});
-      step(s0 + 1, IntTag<1>{}, BoolTag<false>{});
-    }
-    for (; s0 < i1; s0 += 2) {
-      step(s0, IntTag<0>{}, BoolTag<true>{});
-      step(s0 + 1, IntTag<1>{}, BoolTag<true>{});
-    }
-    for (; s0 < steps_pad; s0 += 2) {
-      step(s0, IntTag<0>{}, BoolTag<false>{});
-      step(s0 + 1, IntTag<1>{}, BoolTag<false>{});
-    }
+    auto pair_of_steps = [&](auto interior_tag) {
+      const int ia = (cA0 + s0) & (kCodeRing16 - 1), ib = (cB0 + s0) & (kCodeRing16 - 1);
+      const int it = (s0 + 1) & (kTopRing - 1);
+      step(s0, IntTag<0>{}, interior_tag, ia, ib, it);
+      step(s0 + 1, IntTag<1>{}, interior_tag, ia + 1, ib + 1, it + 1);
+    };
+    for (; s0 < i0; s0 += 2) pair_of_steps(BoolTag<false>{});
+    for (; s0 < i1; s0 += 2) pair_of_steps(BoolTag<true>{});
+    for (; s0 < steps_pad; s0 += 2) pair_of_steps(BoolTag<false>{});
     cp_async_wait_all();
     __syncwarp();
 
