@@ -276,7 +276,10 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       if (vA || vB) {
         uint32_t d = hdiag;
         // F of the lane's first row from the row above it.
-        uint32_t fv = __viaddmax_u16x2(upF, nge2, __viaddmax_u16x2(upH, noe2, kNeg2));
+        // (In the interior every upH is a real cell, far above the floor, so
+        // the subtraction runs as an IMAD on the FMA pipe.)
+        uint32_t fv = __viaddmax_u16x2(upF, nge2,
+                                       INTERIOR ? sub2_imad(upH, one, neg_oe2) : __viaddmax_u16x2(upH, noe2, kNeg2));
         uint32_t xo = 0u;
         // Rows in order.  Since open >= 0, F(i+1,j) = max(F(i,j) - ext,
         // max(X(i,j) [, 0]) - open - ext) with X = max(D + s, E): the only
