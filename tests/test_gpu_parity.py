@@ -2,6 +2,7 @@
 oracle on the same seeded inputs.  Integer work, so the bar is bit-exact:
 scores, coordinates, identity counts and both gapped strings."""
 import ctypes
+import dataclasses
 import json
 import os
 
@@ -179,6 +180,41 @@ def test_invalid_residues_reported_per_pair():
     with pytest.raises(N.TsqError) as e:
         A.align_pair(b"ACGE", b"ACGT", matrix="dna", gap_open=5, gap_extend=2)
     assert e.value.rc == N.E_INVALID_RESIDUE
+
+
+@pytest.mark.parametrize("local,lane", [(False, "auto"), (True, "auto"), (False, "i16")])
+def test_invalid_residues_in_score_batches(local, lane):
+    """Score batches (the int16x2 fill) with invalid bytes planted in some
+    pairs (lowercase, '*', '-', digits, bytes >= 0x80, NUL): exactly those
+    pairs report TSQ_E_INVALID_RESIDUE, every other score equals the
+    oracle's, including pairs whose neighbours in the residue buffer are
+    invalid."""
+    ps = W.uneven_pairs(n_pairs=3000, seed=21)
+    seqs = ps.seqs.copy()
+    rng = np.random.default_rng(22)
+    planted = rng.choice(len(ps), 300, replace=False)
+    junk = np.frombuffer(b"ac*-0\x80\xff\x00z", dtype=np.uint8)
+    for k in planted:
+        off, ln = (ps.a_off[k], ps.a_len[k]) if k % 2 else (ps.b_off[k], ps.b_len[k])
+        seqs[off + rng.integers(ln)] = junk[k % len(junk)]
+    bad = dataclasses.replace(ps, seqs=seqs)
+    got = gpu_batch(bad, local, "score", lane=lane, check=False)
+    is_bad = np.zeros(len(ps), dtype=bool)
+    is_bad[planted] = True
+    assert np.array_equal(got.table["status"] == N.E_INVALID_RESIDUE, is_bad)
+    ok = np.flatnonzero(~is_bad)
+    want = oracle_batch(bad.subset(ok), local, O.MODE_SCORE)
+    assert np.array_equal(got.table["score"][ok], want["score"])
+    # DNA: protein letters are invalid there.
+    dna = W.long_dna_pairs(6, lo=300, hi=600)
+    dseqs = dna.seqs.copy()
+    dseqs[dna.a_off[2] + 5] = ord("E")
+    dbad = dataclasses.replace(dna, seqs=dseqs)
+    got = gpu_batch(dbad, local, "score", lane=lane, check=False)
+    assert got.table["status"].tolist() == [0, 0, N.E_INVALID_RESIDUE, 0, 0, 0]
+    keep = np.array([0, 1, 3, 4, 5])
+    want = oracle_batch(dbad.subset(keep), local, O.MODE_SCORE)
+    assert np.array_equal(got.table["score"][keep], want["score"])
 
 
 def test_bad_arguments_rejected():

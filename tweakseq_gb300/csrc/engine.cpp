@@ -388,7 +388,11 @@ int input_prepare(tsq_batch *owner, int64_t seqs_len, const tsq_params *p, const
   owner->seqs_len = seqs_len;
   TSQ_TRY(owner->seqs.ensure(size_t(seqs_len) + 128, st, owner->async_max));
   TSQ_TRY(owner->codes.ensure(size_t(seqs_len) + 128, st, owner->async_max));
-  if (owner->classes) TSQ_TRY(owner->ccodes.ensure(size_t(seqs_len) + 128, st, owner->async_max));
+  if (owner->classes) {
+    TSQ_TRY(owner->ccodes.ensure(size_t(seqs_len) + 128, st, owner->async_max));
+    // The fills' staging reads up to 64 bytes past a sequence: class 0 there.
+    TSQ_TRY(cudaMemsetAsync(owner->ccodes.as<uint8_t>() + seqs_len, 0, 128, st));
+  }
   TSQ_TRY(owner->lut.ensure(256, st, owner->async_max));
   uint8_t lut[256], clut[256];
   build_lut(sc, lut);
@@ -547,7 +551,11 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   if (!b->input_owner) {
     TSQ_TRY(b->seqs.ensure(size_t(seqs_len) + 128, b->stream, b->async_max));
     TSQ_TRY(b->codes.ensure(size_t(seqs_len) + 128, b->stream, b->async_max));
-    if (b->classes) TSQ_TRY(b->ccodes.ensure(size_t(seqs_len) + 128, b->stream, b->async_max));
+    if (b->classes) {
+      TSQ_TRY(b->ccodes.ensure(size_t(seqs_len) + 128, b->stream, b->async_max));
+      // The fills' staging reads up to 64 bytes past a sequence: class 0 there.
+      TSQ_TRY(cudaMemsetAsync(b->ccodes.as<uint8_t>() + seqs_len, 0, 128, b->stream));
+    }
     if (seqs_len > 0 && !segmented)
       TSQ_TRY(cudaMemcpyAsync(b->seqs.p, seqs, size_t(seqs_len), cudaMemcpyHostToDevice, b->stream));
   }

@@ -137,10 +137,14 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
     qa_codes = A.ccodes + pr.a_off;
     boff = pr.b_off;
   }
-  const uint8_t *qb_codes = A.ccodes + boff;
+  // Invalid residues: their letter codes (class codes of invalid letters
+  // are 0, a valid profile index).
   bool bad = false;
-  for (int k = t; k < m; k += G) bad |= qa_codes[k] >= ncls;
-  for (int k = t; k < n; k += G) bad |= qb_codes[k] >= ncls;
+  if (have) {
+    const uint8_t *la = A.codes + A.pairs[pid].a_off, *lb = A.codes + boff;
+    for (int k = t; k < m; k += G) bad |= la[k] >= kLetters;
+    for (int k = t; k < n; k += G) bad |= lb[k] >= kLetters;
+  }
   const unsigned gm = group_mask_rt(lane, G);
   const bool gbad = (__ballot_sync(0xffffffffu, bad) & gm) != 0;
   const bool trivial = (m == 0 || n == 0 || gbad);
@@ -220,8 +224,8 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
     uint2 pa[2], pb[2];
     uint32_t tv[2];
     {
-      const int ca = min(int(code_ring[(boff - t) & (kCodeRing16 - 1)]), ncls - 1);
-      const int cb = min(int(code_ring[(boff - t - G) & (kCodeRing16 - 1)]), ncls - 1);
+      const int ca = code_ring[(boff - t) & (kCodeRing16 - 1)];
+      const int cb = code_ring[(boff - t - G) & (kCodeRing16 - 1)];
       pa[0] = profA[(2 * ca) * kThreads16];
       pb[0] = profB[(2 * cb) * kThreads16];
       tv[0] = top_ring[0];
@@ -259,8 +263,8 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       const int jA = s - t, jB = jA - G;
       const uint2 wa = pa[k], wb = pb[k];
       {
-        const int ca = min(int(code_ring[ia]), ncls - 1);
-        const int cb = min(int(code_ring[ib]), ncls - 1);
+        const int ca = code_ring[ia];
+        const int cb = code_ring[ib];
         pa[k ^ 1] = profA[(2 * ca) * kThreads16];
         pb[k ^ 1] = profB[(2 * cb) * kThreads16];
       }
@@ -423,6 +427,13 @@ __global__ void __launch_bounds__(kThreads16) fill_i16_kernel(const FillArgs A) 
   uint2 *s_prof = reinterpret_cast<uint2 *>(smem + kMatBytes);
   uint8_t *s_rings = smem + kMatBytes + size_t(2 * A.nclasses) * kThreads16 * sizeof(uint2);
   for (int k = threadIdx.x; k < A.nclasses * A.nclasses; k += blockDim.x) s_mat[k] = A.cmatrix[k];
+  // Code rings start as class 0: a group without a pair still reads its
+  // ring, and the step uses what it reads as a profile index unchecked
+  // (every class code the rings receive is below nclasses).
+  {
+    uint8_t *code_rings = s_rings + kSlots16 * (kTopRing * 4 + kRingPad);
+    for (int k = threadIdx.x; k < kSlots16 * (kCodeRing16 + kRingPad); k += blockDim.x) code_rings[k] = 0;
+  }
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;

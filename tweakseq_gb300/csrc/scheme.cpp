@@ -130,7 +130,9 @@ void build_lut(const Scheme &s, uint8_t lut[256]) {
 }
 
 void build_class_lut(const Scheme &s, uint8_t lut[256]) {
-  for (int c = 0; c < 256; ++c) lut[c] = kBadCode;
+  // Bytes the scheme rejects get class 0 (their letter code marks them
+  // invalid): every class code is a valid profile index.
+  for (int c = 0; c < 256; ++c) lut[c] = 0;
   for (int x = 0; x < kLetters; ++x)
     if (s.valid[x]) lut['A' + x] = s.cls[x];
 }

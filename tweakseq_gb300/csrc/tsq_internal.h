@@ -116,7 +116,8 @@ int build_scheme(const tsq_params *p, Scheme *out);
 // BLOSUM62 entry by row index in the order ARNDCQEGHILKMFPSTWYVBZX.
 int8_t blosum62_by_row(int x, int y);
 void build_lut(const Scheme &s, uint8_t lut[256]);
-// Byte -> score class (kBadCode for bytes the scheme rejects).
+// Byte -> score class (0 for bytes the scheme rejects, which their letter
+// code marks invalid).
 void build_class_lut(const Scheme &s, uint8_t lut[256]);
 
 // Kernel launchers (fill_dispatch.cu, fill_i16.cu, fill_cta.cu, walk_kernel.cu).
