@@ -46,7 +46,10 @@
 namespace tsq {
 namespace fill {
 
-constexpr int kThreads16 = 128;  // 4 warps per block: the profile is 416 bytes per thread
+// 4 warps per block; shared memory (each thread's profile rows, each
+// group's rings) allows 3 blocks per SM.  (2-warp blocks, 14 warps per SM
+// instead of 12, measured no faster: the ALU pipe is the limit.)
+constexpr int kThreads16 = 128;
 constexpr int kSlots16 = kThreads16 / 32 * 8;
 constexpr int kCodeRing16 = 256;  // band B reads codes up to 2G columns behind band A
 constexpr int32_t kNeg16 = -32000;

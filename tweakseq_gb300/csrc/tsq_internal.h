@@ -3,6 +3,10 @@
 // Device data layout (all in HBM, one allocation pool per context):
 //   codes      uint8 per residue: 'A'..'Z' -> 0..25 when the scheme accepts
 //              the letter, kBadCode otherwise (converted once per batch).
+//   ccodes     score batches: uint8 score class per residue, 0 for bytes
+//              the scheme rejects (their codes entry marks them), and 128
+//              bytes of class 0 past the residues: every entry indexes the
+//              int16x2 fill's profile.
 //   pairs      PairDev per pair (offsets into codes, lengths).
 //   tasks      int32 pair ids of one launch, sorted so that the groups of a
 //              warp get pairs of nearly the same shape.
@@ -84,7 +88,7 @@ struct FillArgs {
   int32_t *overflow;     // int16 CHECK: per pair, 1 when a lane came near 32767
   int32_t max_score;     // largest substitution score of the scheme
   uint32_t one;          // int16x2 fill: 1, an opaque multiplier for packed subtractions on the IMAD pipe
-  const uint8_t *ccodes;  // int16x2 fill: class code per residue (kBadCode invalid), same offsets as codes
+  const uint8_t *ccodes;  // int16x2 fill: class code per residue (0 for invalid ones), same offsets as codes
   const int8_t *cmatrix;  // int16x2 fill: nclasses x nclasses class scores
   int32_t nclasses;
 };
