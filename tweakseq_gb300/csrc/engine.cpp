@@ -67,10 +67,10 @@ void DevBuf::release() {
 namespace {
 constexpr size_t kPinMin = size_t(1) << 16;
 constexpr size_t kPinPoolBytes = size_t(8) << 30;
-std::mutex g_pin_mu;
-// (size, block); never destroyed, so buffers released during process exit
-// still find it.
-std::vector<std::pair<size_t, void *>> &g_pin_idle = *new std::vector<std::pair<size_t, void *>>();
+// The lock and the list are never destroyed, so buffers released during
+// process exit (thread-local caches) still find them.
+std::mutex &g_pin_mu = *new std::mutex();
+std::vector<std::pair<size_t, void *>> &g_pin_idle = *new std::vector<std::pair<size_t, void *>>();  // (size, block)
 size_t g_pin_idle_bytes = 0;
 
 size_t pin_class(size_t bytes) {
