@@ -17,10 +17,13 @@ namespace {
 
 // The walk of one pair, from its end cell back to its start, through a
 // plane reader and two sequence readers.  Every lane of the pair's warp runs
-// it with the same values (warp-uniform branches); only `writer` stores.
+// it with the same values (warp-uniform branches); only `writer` (lane 0)
+// stores, except in a run of diagonal moves, where lane k writes the k-th
+// column of the run.
 template <class Plane, class Seq>
 __device__ __forceinline__ void walk_pair(const WalkArgs &A, const PairDev &pr, ResultDev &res, Plane &pl, Seq &a,
-                                          Seq &b, char *out_a, char *out_b, int64_t cap, bool writer) {
+                                          Seq &b, char *out_a, char *out_b, int64_t cap, int lane) {
+  const bool writer = lane == 0;
   const int m = pr.a_len, n = pr.b_len;
   int i, j;
   if (A.local) {
@@ -51,6 +54,32 @@ __device__ __forceinline__ void walk_pair(const WalkArgs &A, const PairDev &pr, 
         if (i == 0 || j == 0 || (pl.nib(j) & 3) == kDirStop) break;
       } else if (i == 0 && j == 0) {
         break;
+      }
+      if (i > 0 && j > 0) {
+        // A run of diagonal moves at once: lane k tests the cell k steps back
+        // along the diagonal, inside the plane window loaded around the
+        // current cell (a cell outside it ends the run); the leading run of
+        // diagonal cells becomes p aligned columns, lane k writing the k-th.
+        (void)pl.nib(j);
+        const uint32_t dm = pl.diag_mask(i, j);
+        const int p = dm == 0xffffffffu ? 32 : __ffs(~dm) - 1;
+        if (p > 1) {
+          a.cover(i - 1);
+          b.cover(j - 1);
+          uint8_t ca = 0, cb = 0;
+          if (lane < p) {
+            ca = a.get(i - 1 - lane);
+            cb = b.get(j - 1 - lane);
+            out_a[cap - L - 1 - lane] = char(ca);
+            out_b[cap - L - 1 - lane] = char(cb);
+          }
+          ident += __popc(__ballot_sync(0xffffffffu, lane < p && ca == cb));
+          L += p;
+          i -= p;
+          j -= p;
+          if (i > 0) pl.set_row(i);
+          continue;
+        }
       }
       if (i == 0) {  // global top row: one horizontal gap run
         ++L;
@@ -187,6 +216,22 @@ struct WarpPlane {
     if (band != wband || t > wt || t <= wt - kWL || s > ws || s <= ws - kWS) refill(s);
     return int(win[(ws - s) * kWL + (wt - t)] >> (4 * r)) & 15;
   }
+  // Lanes whose cell (i - lane, j - lane) lies inside the matrix and the
+  // current window and takes H from the diagonal.
+  __device__ uint32_t diag_mask(int i, int j) const {
+    const int ik = i - lane, jk = j - lane;
+    bool d = false;
+    if (ik >= 1 && jk >= 1) {
+      const int row0 = ik - 1;
+      const int bk = row0 / P;
+      const int w = row0 - bk * P;
+      const int tk = w >> 3, rk = w & 7;
+      const int sk = jk - 1 + tk;
+      if (bk == wband && tk <= wt && tk > wt - kWL && sk <= ws && sk > ws - kWS)
+        d = ((win[(ws - sk) * kWL + (wt - tk)] >> (4 * rk)) & 3) == uint32_t(kDirDiag);
+    }
+    return __ballot_sync(0xffffffffu, d);
+  }
 };
 
 // One sequence read backwards through a shared window of kSeqWin residues.
@@ -196,22 +241,29 @@ struct WarpSeq {
   uint8_t *win;
   int lane;
   int lo = 1 << 30;
-  __device__ uint8_t at(int idx) {
-    if (idx < lo || idx >= lo + kSeqWin) {
-      lo = max(0, idx - kSeqWin + 1);
-      uint8_t v[kSeqWin / 32];
+  // The window ending at idx.
+  __device__ void refill_to(int idx) {
+    lo = max(0, idx - kSeqWin + 1);
+    uint8_t v[kSeqWin / 32];
 #pragma unroll
-      for (int q = 0; q < kSeqWin / 32; ++q) {
-        const int k = lo + lane + 32 * q;
-        v[q] = k < len ? base[k] : uint8_t(0);
-      }
-      __syncwarp();
-#pragma unroll
-      for (int q = 0; q < kSeqWin / 32; ++q) win[lane + 32 * q] = v[q];
-      __syncwarp();
+    for (int q = 0; q < kSeqWin / 32; ++q) {
+      const int k = lo + lane + 32 * q;
+      v[q] = k < len ? base[k] : uint8_t(0);
     }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < kSeqWin / 32; ++q) win[lane + 32 * q] = v[q];
+    __syncwarp();
+  }
+  __device__ uint8_t at(int idx) {
+    if (idx < lo || idx >= lo + kSeqWin) refill_to(idx);
     return win[idx - lo];
   }
+  // Makes residues idx-31..idx (those >= 0) readable with get().
+  __device__ void cover(int idx) {
+    if (max(0, idx - 31) < lo || idx >= lo + kSeqWin) refill_to(idx);
+  }
+  __device__ uint8_t get(int idx) const { return win[idx - lo]; }
 };
 
 __global__ void __launch_bounds__(kWarpWalkWarps * 32) walk_warp_kernel(const WalkArgs A) {
@@ -230,7 +282,7 @@ __global__ void __launch_bounds__(kWarpWalkWarps * 32) walk_warp_kernel(const Wa
   const int G = A.shape_G[p];
   WarpPlane pl{reinterpret_cast<const uint32_t *>(A.planes + A.plane_off[p]), s_plane[w], pr.b_len, G,
                G * A.shape_R[p], lane};
-  walk_pair(A, pr, res, pl, a, b, out_a, out_a + cap, cap, lane == 0);
+  walk_pair(A, pr, res, pl, a, b, out_a, out_a + cap, cap, lane);
 }
 
 // ASCII -> letter codes, and (when clut is set) -> score classes for the
