@@ -259,3 +259,33 @@ def test_identity_distance():
     assert O.lib().tsqo_identity_distance(1, 3) == ((2 << 32) // 3)
     D = O.identity_distances(3, [1, 2, 3], [2, 2, 4])
     assert D[0, 1] == 1 << 31 and D[0, 2] == 0 and D[1, 2] == (1 << 32) // 4 and D[2, 1] == D[1, 2]
+
+
+@pytest.mark.parametrize("method", [O.TREE_UPGMA, O.TREE_NJ])
+def test_tree_text_and_leaf_order(method):
+    """msa.Tree's Newick text and leaf order (host logic over the join list)
+    on trees the oracle builds: every leaf once, one pair of parentheses per
+    join, branch lengths as length / 2^32, and leaf order matching the
+    Newick leaves read left to right."""
+    import re
+
+    from tweakseq_gb300 import msa
+
+    rng = np.random.default_rng(41 + method)
+    n = 23
+    x = rng.random((n, 3))
+    d = np.sqrt(((x[:, None, :] - x[None, :, :]) ** 2).sum(-1))
+    D = np.round(d * (1 << 32)).astype(np.int64)
+    nodes = O.guide_tree(D, method)
+    tree = msa.Tree(n, nodes, "upgma" if method == O.TREE_UPGMA else "nj")
+    labels = [f"s{k}" for k in range(n)]
+    text = tree.newick(labels)
+    assert text.endswith(";") and text.count("(") == text.count(")") == n - 1
+    leaves = re.findall(r"[(,](s\d+):", text)
+    assert sorted(leaves) == sorted(labels)
+    assert [labels[k] for k in tree.leaf_order()] == leaves
+    lengths = [float(v) for v in re.findall(r":(-?\d+\.\d+)", text)]
+    want = sorted(float(f"{v / (1 << 32):.6f}") for v in np.concatenate([nodes["left_length"], nodes["right_length"]]))
+    assert sorted(lengths) == want
+    one = msa.Tree(1, np.zeros(0, dtype=O.TREE_NODE_DTYPE), "upgma")
+    assert one.newick(["only"]) == "only;" and one.leaf_order() == [0]
