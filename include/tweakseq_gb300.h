@@ -105,7 +105,10 @@ typedef struct {
   int32_t device;       /* CUDA ordinal; -1 = current device */
   int32_t use_graph;    /* 1 = replay the launch sequence as a CUDA graph */
   int32_t autotune;     /* 1 = consult the tuned table (tsq_tune_load) */
-  int32_t reserved;
+  int32_t wait_polls;   /* polls a bounded device-side wait makes before it
+                           gives up and its pair reports TSQ_E_TIMEOUT (the
+                           long-pair fill's warps wait on one another);
+                           0 = the default, 4,194,304 */
 } tsq_batch_opts;
 
 /* Counters of the last run of a batch. */
@@ -252,8 +255,12 @@ typedef struct {
  * (larger values return TSQ_E_TOO_LARGE); a pair longer than max_len or
  * outside the residue buffer gets status TSQ_E_TOO_LARGE / TSQ_E_INVALID_ARG
  * in d_out.  p->output must be TSQ_OUT_SCORE; p->lane is ignored (int32).
+ * d_seqs must be 16-byte aligned (the residues are read 16 bytes at a
+ * time), d_pairs 8-byte and d_out 4-byte aligned; a misaligned pointer is
+ * refused with TSQ_E_INVALID_ARG before anything is launched.
  * The first call on a device sets up the device address of the array and
- * should come before any stream capture.  Calls share the array: two calls
+ * should come before any stream capture; that set-up lasts for the process
+ * and is not redone after cudaDeviceReset.  Calls share the array: two calls
  * that overlap on the GPU race and corrupt each other's results. */
 int tsq_align_score_noalloc(const uint8_t *d_seqs, int64_t seqs_len,
                             const tsq_pair_desc *d_pairs, int32_t n,

@@ -265,3 +265,17 @@ def guide_tree(dist: np.ndarray, method: int = TREE_UPGMA) -> np.ndarray:
     if rc:
         raise OracleError(rc)
     return out[:max(n - 1, 0)]
+
+
+def threads_for_traceback(max_cells: int, cap: int = 0) -> int:
+    """Host threads for a traceback batch whose largest pair has max_cells
+    cells: the oracle's direction matrix takes one byte per cell per thread,
+    so the count is bounded by the memory available now (with a 1.5x margin)
+    as well as by the host cores (and by cap when it is set)."""
+    try:
+        avail = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+    except (ValueError, OSError, AttributeError):
+        avail = 8 << 30
+    by_ram = int(avail // max(1, int(1.5 * max_cells)))
+    n = max(1, min(num_cores(), by_ram))
+    return min(n, cap) if cap > 0 else n

@@ -1,6 +1,6 @@
 """Regenerates the committed golden fixtures.  Run explicitly:
 
-    python tests/golden/make_golden.py [--reference-root DIR]
+    python tests/golden/make_golden.py --reference-root DIR
 
 1. ``blosum62_reference.json`` -- the BLOSUM62 table and its 'A'..'Z' index
    map, parsed from the reference's own source text,
@@ -114,15 +114,15 @@ def oracle_cases() -> list[dict]:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference-root", default="/root/reference")
+    ap.add_argument("--reference-root", required=True,
+                    help="root of the groundstate/tweakseq source tree (holds tweakseq/Core/...)")
     args = ap.parse_args()
     cpp = os.path.join(args.reference_root, "tweakseq/Core/Annotations/Consensus.cpp")
-    if os.path.exists(cpp):
-        with open(os.path.join(HERE, "blosum62_reference.json"), "w") as f:
-            json.dump(parse_consensus_cpp(cpp), f, indent=1)
-        print("wrote blosum62_reference.json")
-    else:
-        print("reference tree absent: blosum62_reference.json left as it is")
+    if not os.path.exists(cpp):
+        raise SystemExit(f"{cpp} not found: --reference-root must name the reference source tree")
+    with open(os.path.join(HERE, "blosum62_reference.json"), "w") as f:
+        json.dump(parse_consensus_cpp(cpp), f, indent=1)
+    print("wrote blosum62_reference.json")
     with open(os.path.join(HERE, "oracle_cases.json"), "w") as f:
         json.dump(oracle_cases(), f, indent=1)
     print("wrote oracle_cases.json")

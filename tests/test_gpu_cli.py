@@ -45,7 +45,52 @@ def test_pairwise_fasta_round_trip(tmp_path):
     assert tool.align_files(str(fin), str(fout), local=True, dna=True).returncode == 0
     got = F.read(str(fout))
     want = O.align(b"ACGTACGTTTGACCAACGT", b"TTACGACGTTAGACNCA", O.DNA, 5, 2, True)
-    assert (got[0].sequence, got[1].sequence) == (want.aln_a, want.aln_b)
+    _check_full_local_rows(got, "ACGTACGTTTGACCAACGT", "TTACGACGTTAGACNCA", want)
+
+
+def _check_full_local_rows(recs, a, b, want):
+    """Full-length local rows: equal length, each row without its gaps is
+    its whole input sequence, and the columns between the flanks are the
+    oracle's local alignment."""
+    ra, rb = recs[0].sequence, recs[1].sequence
+    assert len(ra) == len(rb)
+    assert ra.replace("-", "") == a and rb.replace("-", "") == b
+    lead = want.a_begin + want.b_begin
+    assert ra[:lead] == a[:want.a_begin] + "-" * want.b_begin
+    assert rb[:lead] == "-" * want.a_begin + b[:want.b_begin]
+    assert ra[lead:lead + want.n_cols] == want.aln_a and rb[lead:lead + want.n_cols] == want.aln_b
+    tail_a, tail_b = len(a) - want.a_end, len(b) - want.b_end
+    assert ra[lead + want.n_cols:] == a[want.a_end:] + "-" * tail_b
+    assert rb[lead + want.n_cols:] == "-" * tail_a + b[want.b_end:]
+    assert len(ra) == lead + want.n_cols + tail_a + tail_b
+
+
+def test_local_mode_keeps_whole_sequences(tmp_path):
+    """The editor replaces each sequence with the row it reads back
+    (Project::readNewAlignment), so local output must keep the unaligned
+    flanks: protein pairs with a shared core inside unrelated flanks, a pair
+    with no positive cell (empty local alignment) and a pair aligned from
+    its first residues."""
+    rng = np.random.default_rng(41)
+    tool = T.GpuAlignmentTool()
+    fin, fout = tmp_path / "in.fa", tmp_path / "out.fa"
+    cases = []
+    for k in range(6):
+        core = W.random_protein(rng, int(rng.integers(40, 160)))
+        mut, _ = W._mutate_proteins(rng, core, np.array([len(core)]), np.array([0.3]), 0.05)
+        fa = W.random_protein(rng, int(rng.integers(0, 90))).tobytes().decode()
+        fb = W.random_protein(rng, int(rng.integers(0, 90))).tobytes().decode()
+        ta = W.random_protein(rng, int(rng.integers(0, 90))).tobytes().decode()
+        tb = W.random_protein(rng, int(rng.integers(0, 90))).tobytes().decode()
+        cases.append((fa + core.tobytes().decode() + ta, fb + mut.tobytes().decode() + tb))
+    cases.append(("PPPPPPPP", "WWWWW"))  # every cell scores below zero: empty local alignment
+    cases.append(("HEAGAWGHEE", "HEAGAWGHEEPAWHEAE"))
+    for a, b in cases:
+        F.write(str(fin), [F.Record(">a", "a", a), F.Record(">b", "b", b)])
+        r = tool.align_files(str(fin), str(fout), local=True)
+        assert r.returncode == 0, r.stderr
+        want = O.align(a.encode(), b.encode(), local=True)
+        _check_full_local_rows(F.read(str(fout)), a, b, want)
 
 
 def test_all_vs_all_identity_table(tmp_path):

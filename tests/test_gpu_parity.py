@@ -449,3 +449,47 @@ def test_chunked_call_reports_the_first_bad_pair():
     # The engines are usable again afterwards.
     ok = A.align_batch(ps.subset(np.arange(40000)), output="score")
     assert (ok.table["status"] == 0).all()
+
+
+@pytest.mark.parametrize("output", ["alignment", "score"])
+def test_cta_wait_runs_out_then_engine_recovers(output):
+    """The long-pair fill's warps wait on one another with bounded polls.
+    With the limit set to a single poll the waits run out: the kernel still
+    returns, the long pair reports TSQ_E_TIMEOUT, the short pairs of the
+    same call (warp-per-pair fills) are unaffected, and the next call on the
+    same cached engine, with the default limit, is bit-exact."""
+    rng = np.random.default_rng(57)
+    seqs, pairs = [], []
+    a = W.DNA_LETTERS[rng.integers(0, 4, 20000)]
+    seqs += [a.tobytes(), W._mutate_dna(rng, a, 0.1, 0.02, 3.0)[:3000].tobytes()]
+    pairs.append((0, 1))
+    for k in range(30):
+        x = W.DNA_LETTERS[rng.integers(0, 4, int(rng.integers(50, 400)))]
+        seqs += [x.tobytes(), W._mutate_dna(rng, x, 0.1, 0.02, 3.0).tobytes()]
+        pairs.append((len(seqs) - 2, len(seqs) - 1))
+    ps = W._pairset_from_lists(seqs, pairs, matrix=W.DNA, gap_open=5, gap_extend=2)
+    kw = dict(matrix="dna", gap_open=5, gap_extend=2, output=output)
+    mode = O.MODE_ALIGN if output == "alignment" else O.MODE_SCORE
+    want = O.batch(ps.seqs, ps.a_off, ps.a_len, ps.b_off, ps.b_len, O.DNA, 5, 2, False, mode, 0, mode == O.MODE_ALIGN)
+    if mode == O.MODE_ALIGN:
+        want, sa, sb = want
+    with pytest.raises(N.TsqError) as e:
+        A.align_batch(ps, wait_polls=1, **kw)
+    assert e.value.rc == N.E_TIMEOUT
+    got = A.align_batch(ps, wait_polls=1, check=False, **kw)
+    assert got.table["status"][0] == N.E_TIMEOUT
+    assert (got.table["status"][1:] == 0).all()
+    assert np.array_equal(got.table["score"][1:], want["score"][1:])
+    # The same engine, default limit: every pair bit-exact.
+    got = A.align_batch(ps, **kw)
+    assert (got.table["status"] == 0).all()
+    assert np.array_equal(got.table["score"], want["score"])
+    if mode == O.MODE_ALIGN:
+        assert got.aln_a == sa and got.aln_b == sb
+    # A device-resident batch with a short limit times out on every run and
+    # keeps running.
+    with A.Batch(ps, use_graph=False, wait_polls=1, **kw) as b:
+        for _ in range(2):
+            b.run()
+            r = b.results(check=False)
+            assert r.table["status"][0] == N.E_TIMEOUT and (r.table["status"][1:] == 0).all()

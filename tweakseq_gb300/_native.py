@@ -77,7 +77,7 @@ class PairDesc(ctypes.Structure):
 
 class BatchOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("use_graph", ctypes.c_int32), ("autotune", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("wait_polls", ctypes.c_int32)]
 
 
 class ServerOpts(ctypes.Structure):

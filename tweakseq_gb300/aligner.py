@@ -135,21 +135,22 @@ def _as_inputs(pairs):
     return seqs, pair_table(a_off, a_len, b_off, b_len)
 
 
-def _opts(use_graph=False, autotune=False, device=-1) -> N.BatchOpts:
+def _opts(use_graph=False, autotune=False, device=-1, wait_polls=0) -> N.BatchOpts:
     o = N.BatchOpts()
     o.device, o.use_graph, o.autotune = int(device), int(bool(use_graph)), int(bool(autotune))
+    o.wait_polls = int(wait_polls)
     return o
 
 
 def align_batch(pairs, matrix="blosum62", gap_open=11, gap_extend=1, mode="global", output="alignment",
-                lane="auto", custom=None, use_graph=False, autotune=False, check=True) -> BatchResult:
+                lane="auto", custom=None, use_graph=False, autotune=False, check=True, wait_polls=0) -> BatchResult:
     """Batched form: all pairs in one planned launch sequence.  Host buffers
     in, host results out (the copies are part of the call)."""
     L = N.lib()
     seqs, tab = _as_inputs(pairs)
     p, keep = N.make_params(matrix, gap_open, gap_extend, mode, output, lane, custom)
     raw = np.zeros(len(tab), dtype=N.RESULT_DTYPE)
-    o = _opts(use_graph, autotune)
+    o = _opts(use_graph, autotune, wait_polls=wait_polls)
     rc = L.tsq_align_batch(seqs.ctypes.data if len(seqs) else None, len(seqs), tab.ctypes.data if len(tab) else None,
                            len(tab), ctypes.byref(p), ctypes.byref(o), raw.ctypes.data if len(raw) else None)
     if rc not in (N.TSQ_OK, N.E_INVALID_RESIDUE):
@@ -166,11 +167,11 @@ class Batch:
     number of runs; results stay in HBM until ``results()``."""
 
     def __init__(self, pairs, matrix="blosum62", gap_open=11, gap_extend=1, mode="global", output="score",
-                 lane="auto", custom=None, use_graph=True, autotune=False):
+                 lane="auto", custom=None, use_graph=True, autotune=False, wait_polls=0):
         L = N.lib()
         seqs, tab = _as_inputs(pairs)
         p, keep = N.make_params(matrix, gap_open, gap_extend, mode, output, lane, custom)
-        o = _opts(use_graph, autotune)
+        o = _opts(use_graph, autotune, wait_polls=wait_polls)
         h = ctypes.c_void_p()
         rc = L.tsq_batch_create(seqs.ctypes.data if len(seqs) else None, len(seqs),
                                 tab.ctypes.data if len(tab) else None, len(tab), ctypes.byref(p), ctypes.byref(o),

@@ -12,6 +12,9 @@
 //   two sequences  -> their pairwise alignment as gapped FASTA, same labels
 //                     and header lines, 80 residues per line (the editor's
 //                     own FASTA writer wraps at 80, FASTAFile.cpp:149-171);
+//                     with --local each row still holds its whole input
+//                     sequence: the unaligned flanks stand against gaps
+//                     around the aligned core (full_local_rows below);
 //   --all-vs-all   -> every unordered pair, one TSV line per pair: labels,
 //                     score, identical columns, columns, percent identity
 //                     (the distance input of a guide tree);
@@ -117,6 +120,20 @@ std::string newick(const std::vector<tsq_tree_node> &nodes, const std::vector<Re
     text[size_t(n + t)] = "(" + text[size_t(nd.left)] + la + "," + text[size_t(nd.right)] + lb + ")";
   }
   return (n == 1 ? text[0] : text[size_t(2 * n - 2)]) + ";";
+}
+
+// Full-length rows of a local alignment: every residue of a and of b appears
+// in its row, in order, so that removing the gaps gives the input back.
+// Columns, left to right: a[0:a_begin] over gaps, gaps over b[0:b_begin],
+// the aligned core (aln_a over aln_b), a[a_end:] over gaps, gaps over
+// b[b_end:].  An empty local alignment (score 0, coordinates 0) gives a over
+// gaps followed by gaps over b.
+void full_local_rows(const std::string &a, const std::string &b, const tsq_result &r, std::string &row_a,
+                     std::string &row_b) {
+  const size_t ab = size_t(r.a_begin), ae = size_t(r.a_end), bb = size_t(r.b_begin), be = size_t(r.b_end);
+  const std::string core_a = r.aln_a ? r.aln_a : "", core_b = r.aln_b ? r.aln_b : "";
+  row_a = a.substr(0, ab) + std::string(bb, '-') + core_a + a.substr(ae) + std::string(b.size() - be, '-');
+  row_b = std::string(ab, '-') + b.substr(0, bb) + core_b + std::string(a.size() - ae, '-') + b.substr(be);
 }
 
 const char *status_name(int rc) {
@@ -262,8 +279,21 @@ int main(int argc, char **argv) {
       std::fprintf(stderr, "tsq_align: %s\n", status_name(rc));
       return 1;
     }
-    write_wrapped(*out, recs[0].header, r.aln_a);
-    write_wrapped(*out, recs[1].header, r.aln_b);
+    if (p.mode == TSQ_LOCAL) {
+      // The editor replaces each sequence's residues with the row it reads
+      // back (Project::readNewAlignment, tweakseq/Core/Project.cpp:1016), so
+      // a row must hold the whole input sequence.  Full-length local rows:
+      // a's unaligned prefix against gaps, then b's unaligned prefix against
+      // gaps, the aligned core, a's unaligned suffix against gaps, then b's
+      // unaligned suffix against gaps.
+      std::string row_a, row_b;
+      full_local_rows(a, b, r, row_a, row_b);
+      write_wrapped(*out, recs[0].header, row_a);
+      write_wrapped(*out, recs[1].header, row_b);
+    } else {
+      write_wrapped(*out, recs[0].header, r.aln_a);
+      write_wrapped(*out, recs[1].header, r.aln_b);
+    }
     tsq_result_free(&r);
     return 0;
   }

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "trace.h"
 
 namespace {
 
@@ -112,7 +113,7 @@ int align_in_chunks(ThreadCache &c, tsq_batch *e, const uint8_t *seqs, int64_t s
     if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return TSQ_E_CUDA;
     c.seg_events.push_back(ev);
   }
-  const tsq_batch_opts o{dev, 0, opts ? opts->autotune : 0, 0};
+  const tsq_batch_opts o{dev, 0, opts ? opts->autotune : 0, opts ? opts->wait_polls : 0};
 
   cudaPointerAttributes attr{};
   const bool in_place = seqs_len > 0 && cudaPointerGetAttributes(&attr, seqs) == cudaSuccess &&
@@ -307,6 +308,7 @@ int64_t tsq_results_strings(const tsq_result *r, int64_t n, char *buf, int64_t b
 
 int tsq_align_pair(const uint8_t *a, int32_t la, const uint8_t *b, int32_t lb, const tsq_params *p,
                    tsq_result *out) {
+  tsq::TraceRange tr("tsq_align_pair");
   return guarded([&]() -> int {
     if (!out || !p || la < 0 || lb < 0 || (la > 0 && !a) || (lb > 0 && !b)) return TSQ_E_INVALID_ARG;
     std::memset(out, 0, sizeof(*out));
@@ -333,6 +335,7 @@ int tsq_align_pair(const uint8_t *a, int32_t la, const uint8_t *b, int32_t lb, c
 
 int tsq_align_batch(const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *pairs, int64_t n,
                     const tsq_params *p, const tsq_batch_opts *opts, tsq_result *out) {
+  tsq::TraceRange tr("tsq_align_batch");
   return guarded([&]() -> int {
     if (n > 0 && !out) return TSQ_E_INVALID_ARG;
     int dev = 0;

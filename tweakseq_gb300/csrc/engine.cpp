@@ -8,6 +8,7 @@
 // one fill launch per bucket, and (alignment output) the traceback walk.
 // The run can be captured once as a CUDA graph and replayed.
 #include "engine.h"
+#include "trace.h"
 
 #include <algorithm>
 #include <array>
@@ -344,6 +345,7 @@ int out_mode_of(const tsq_params *p) {
 
 int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *pairs, int64_t n,
                const tsq_params *p, const tsq_batch_opts *opts, bool plain) {
+  TraceRange tr(plain ? "plan (one pair)" : "plan");
   return plan_impl(b, nullptr, seqs, seqs_len, pairs, n, p, opts, plain, 0, 0, false);
 }
 
@@ -351,9 +353,10 @@ int batch_plan_chunk(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, 
                      const tsq_pair_desc *pairs, int64_t n, const tsq_params *p, const tsq_batch_opts *opts,
                      int64_t call_pairs, int64_t call_cells, bool segmented) {
   if (!b || owner == b || call_pairs < n || call_cells < 0) return TSQ_E_INVALID_ARG;
+  TraceRange tr("plan chunk");
   if (!owner)
     return plan_impl(b, nullptr, seqs, seqs_len, pairs, n, p, opts, false, call_pairs, call_cells, segmented);
-  const tsq_batch_opts o{owner->device, 0, opts ? opts->autotune : 0, 0};
+  const tsq_batch_opts o{owner->device, 0, opts ? opts->autotune : 0, opts ? opts->wait_polls : 0};
   return plan_impl(b, owner, nullptr, owner->seqs_len, pairs, n, p, &o, false, call_pairs, call_cells, segmented);
 }
 
@@ -476,6 +479,7 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   b->local = p->mode == TSQ_LOCAL;
   b->use_graph = opts ? opts->use_graph != 0 : false;
   b->autotune = opts ? opts->autotune != 0 : false;
+  b->wait_polls = opts && opts->wait_polls > 0 ? opts->wait_polls : 0;
   b->n = n;
   b->seqs_len = seqs_len;
   b->has_run = false;
@@ -914,7 +918,17 @@ cudaError_t record(tsq_batch *b, int k) {
                       : cudaEventRecord(b->ev[k], b->stream);
 }
 
+// Fill launch names for the trace ranges: [i16][out_mode].
+const char *fill_range_name(const Launch &L, int out_mode) {
+  if (L.cta) return out_mode == kOutTrace ? "fill_cta trace" : (out_mode == kOutIdent ? "fill_cta identity" : "fill_cta score");
+  if (L.rerun) return "fill_i32 re-run of int16 overflows";
+  if (L.i16 == 1) return "fill_i16 score";
+  if (L.i16 == 2) return "fill_i16 score (checked)";
+  return out_mode == kOutTrace ? "fill_i32 trace" : (out_mode == kOutIdent ? "fill_i32 identity" : "fill_i32 score");
+}
+
 int enqueue_run(tsq_batch *b) {
+  TraceRange tr("enqueue run");
   cudaStream_t st = b->stream;
   const int nl = int(b->launches.size());
   TSQ_TRY(cudaMemsetAsync(b->counters.p, 0, sizeof(int32_t) * (size_t(nl) + 2), st));
@@ -927,6 +941,7 @@ int enqueue_run(tsq_batch *b) {
     // The owner encodes the residues on its stream.
     TSQ_TRY(cudaStreamWaitEvent(st, b->input_owner->ev_encoded, 0));
   } else {
+    TraceRange er("encode");
     TSQ_TRY(launch_encode(b->seqs.as<uint8_t>(), b->seqs_len, b->lut.as<uint8_t>(), b->codes.as<uint8_t>(),
                           b->classes ? b->clut.as<uint8_t>() : nullptr, b->classes ? b->ccodes.as<uint8_t>() : nullptr,
                           st));
@@ -943,6 +958,7 @@ int enqueue_run(tsq_batch *b) {
   }
   for (int l = 0; l < nl; ++l) {
     const Launch &L = b->launches[size_t(l)];
+    TraceRange lr(fill_range_name(L, b->out_mode));
     if (L.cta) {
       FillArgs a{};
       a.codes = codes_dev(b);
@@ -959,6 +975,7 @@ int enqueue_run(tsq_batch *b) {
       a.planes = b->planes.as<uint8_t>();
       a.plane_off = b->plane_off.as<int64_t>();
       a.max_score = b->scheme.max_score;
+      a.spin_limit = b->wait_polls;
       TSQ_TRY(launch_cta(b->out_mode, b->local, a, L.blocks, b->side));
       continue;
     }
@@ -1015,6 +1032,7 @@ int enqueue_run(tsq_batch *b) {
     w.res = b->res.as<ResultDev>();
     w.aln = b->aln.as<char>();
     w.aln_off = b->aln_off.as<int64_t>();
+    TraceRange wr("walk");
     TSQ_TRY(launch_walk(w, st));
   }
   TSQ_TRY(record(b, 3));
@@ -1025,6 +1043,7 @@ int enqueue_run(tsq_batch *b) {
 
 int batch_run_async(tsq_batch *b) {
   if (!b) return TSQ_E_INVALID_ARG;
+  TraceRange tr(b->use_graph ? "batch run (graph)" : "batch run");
   TSQ_TRY(cudaSetDevice(b->device));
   if (!b->use_graph) {
     const int rc = enqueue_run(b);
@@ -1055,6 +1074,7 @@ int batch_run_async(tsq_batch *b) {
 
 int batch_sync(tsq_batch *b) {
   if (!b) return TSQ_E_INVALID_ARG;
+  TraceRange tr("batch sync");
   TSQ_TRY(cudaStreamSynchronize(b->stream));
   if (!b->has_run) return TSQ_OK;
   b->stats.rerun_pairs = b->n_checked > 0 ? *b->rerun_h.as<int32_t>() : 0;

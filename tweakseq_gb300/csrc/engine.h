@@ -116,6 +116,7 @@ struct tsq_batch {
   bool local = false;
   bool use_graph = false;
   bool autotune = false;
+  int32_t wait_polls = 0;  // CTA fill: polls per bounded wait (0 = default)
   int64_t n = 0;
   int64_t seqs_len = 0;
   int64_t cells = 0;

@@ -14,9 +14,12 @@
 // stages that row with cp.async as the warp-per-pair fill does, after
 // checking warp 7's progress counter.
 //
-// Every wait is bounded (kSpinLimit polls); a wait that runs out marks the
-// pair TSQ_E_TIMEOUT and makes every other wait of the CTA give up, so the
-// kernel always finishes.
+// Every wait is bounded (FillArgs::spin_limit polls, kSpinLimit when it is
+// 0); a wait that runs out marks the pair TSQ_E_TIMEOUT and makes every
+// other wait of the CTA give up, so the kernel always finishes.  A warp
+// whose wait gave up carries on without waiting: every index it uses stays
+// inside its rings, its rows and its pair's planes, and the pair's results
+// are discarded through its status.
 #pragma once
 
 #include <algorithm>
@@ -52,9 +55,9 @@ __host__ __device__ constexpr size_t cta_smem_bytes(int out_mode) {
 
 // Warp-uniform poll of a shared counter until it reaches target.  False if
 // the wait ran out (or another wait of the CTA did).
-__device__ __forceinline__ bool cta_wait_geq(const volatile int *ctr, int target, volatile int *fail) {
+__device__ __forceinline__ bool cta_wait_geq(const volatile int *ctr, int target, volatile int *fail, int limit) {
   const int lane = threadIdx.x & 31;
-  for (int it = 0; it < kSpinLimit; ++it) {
+  for (int it = 0; it < limit; ++it) {
     int v = 0, f = 0;
     if (lane == 0) {
       v = *ctr;
@@ -103,6 +106,7 @@ __global__ void __launch_bounds__(kCtaThreads, 1) fill_cta_kernel(const FillArgs
   uint8_t *code_ring = code_rings + w * (kCodeRing + kRingPad);
   const uint2 *prof = s_prof + threadIdx.x;
   const int n_tasks = A.n_wtasks_dev ? *A.n_wtasks_dev : A.n_wtasks;
+  const int spin = A.spin_limit > 0 ? A.spin_limit : kSpinLimit;
 
   for (;;) {
     if (threadIdx.x == 0) s_misc[0] = atomicAdd(A.counter, 1);
@@ -195,7 +199,7 @@ __global__ void __launch_bounds__(kCtaThreads, 1) fill_cta_kernel(const FillArgs
       // Where this band's top row comes from.  Warp 0: the global row (row
       // 0, or warp 7's previous band, whose progress it checks first).
       auto stage_global = [&](int chunk) {
-        if (band > 0) cta_wait_geq(&prod[0], (i - 1) * n + min(kChunk * (chunk + 1), n), fail);
+        if (band > 0) cta_wait_geq(&prod[0], (i - 1) * n + min(kChunk * (chunk + 1), n), fail, spin);
         stage_chunk<G, Top>(chunk, t, n, grow, stage_ring, A.codes, boff, code_ring);
       };
       cp_async_wait_all();
@@ -204,7 +208,7 @@ __global__ void __launch_bounds__(kCtaThreads, 1) fill_cta_kernel(const FillArgs
         stage_global(0);
       } else {
         stage_codes(0, t, n, A.codes, boff, code_ring);
-        cta_wait_geq(&prod[w], base + min(kChunk + 1, n), fail);
+        cta_wait_geq(&prod[w], base + min(kChunk + 1, n), fail, spin);
       }
       cp_async_commit();
       cp_async_wait_all();
@@ -215,7 +219,7 @@ __global__ void __launch_bounds__(kCtaThreads, 1) fill_cta_kernel(const FillArgs
         stage_codes(1, t, n, A.codes, boff, code_ring);
       cp_async_commit();
       // Producer side: room for the first chunk of this band's bottom row.
-      if (out_ring) cta_wait_geq(&cons[w + 1], base + kChunk - kCtaRing, fail);
+      if (out_ring) cta_wait_geq(&cons[w + 1], base + kChunk - kCtaRing, fail, spin);
 
       auto top_at = [&](int col) -> Top {
         return w == 0 ? stage_ring[col & (kTopRing - 1)] : ring_in[(base + col) % kCtaRing];
@@ -249,7 +253,7 @@ __global__ void __launch_bounds__(kCtaThreads, 1) fill_cta_kernel(const FillArgs
               __threadfence_block();  // the entries read so far are in registers
               cons[w] = base + min(s + 2, n);
             }
-            cta_wait_geq(&prod[w], base + min(s + 1 + kChunk + 1, n), fail);
+            cta_wait_geq(&prod[w], base + min(s + 1 + kChunk + 1, n), fail, spin);
           }
           cp_async_commit();
         }
@@ -264,7 +268,7 @@ __global__ void __launch_bounds__(kCtaThreads, 1) fill_cta_kernel(const FillArgs
             else
               prod[w + 1] = base + done;
           }
-          if (out_ring && done < n) cta_wait_geq(&cons[w + 1], base + done + kChunk - kCtaRing, fail);
+          if (out_ring && done < n) cta_wait_geq(&cons[w + 1], base + done + kChunk - kCtaRing, fail, spin);
         }
         int32_t upH = __shfl_up_sync(0xffffffffu, outH, 1);
         int32_t upF = __shfl_up_sync(0xffffffffu, outF, 1);

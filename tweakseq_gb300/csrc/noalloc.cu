@@ -26,7 +26,14 @@
 // Set-up: the first call on a device looks up the array's device address
 // with cudaGetSymbolAddress (the host-side symbol is a stand-in, never a
 // device address) and opts the fill kernel into its shared memory; that
-// first call should come before any stream capture.
+// first call should come before any stream capture.  The set-up is kept per
+// device for the life of the process: it is not redone after
+// cudaDeviceReset, so a process that resets a device must not call this
+// entry point on it again.
+//
+// Alignment: d_seqs must be 16-byte aligned, d_pairs 8-byte and d_out
+// 4-byte aligned; other pointers are refused with TSQ_E_INVALID_ARG.
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 
@@ -166,6 +173,13 @@ extern "C" int tsq_align_score_noalloc(const uint8_t *d_seqs, int64_t seqs_len, 
   if (!p || n < 0 || seqs_len < 0 || max_len < 0) return TSQ_E_INVALID_ARG;
   if (seqs_len > kMaxResidues || int64_t(n) > kMaxPairs || max_len > kMaxLen) return TSQ_E_TOO_LARGE;
   if ((seqs_len > 0 && !d_seqs) || (n > 0 && (!d_pairs || !d_out))) return TSQ_E_INVALID_ARG;
+  // The encoder reads the residues 16 bytes at a time, the pair table holds
+  // 8-byte offsets and the results are 4-byte fields: a misaligned caller
+  // pointer (an offset into the caller's own buffer, say) is refused here,
+  // before anything is launched, instead of faulting on the device.
+  if ((seqs_len > 0 && (reinterpret_cast<uintptr_t>(d_seqs) & 15u) != 0) ||
+      (n > 0 && ((reinterpret_cast<uintptr_t>(d_pairs) & 7u) != 0 || (reinterpret_cast<uintptr_t>(d_out) & 3u) != 0)))
+    return TSQ_E_INVALID_ARG;
   if (p->output != TSQ_OUT_SCORE || (p->mode != TSQ_GLOBAL && p->mode != TSQ_LOCAL)) return TSQ_E_INVALID_ARG;
   if (p->gap_open < 0 || p->gap_extend < 0 || p->gap_open > 1000000 || p->gap_extend > 1000000)
     return TSQ_E_INVALID_ARG;

@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "trace.h"
 
 namespace {
 
@@ -121,6 +122,7 @@ struct tsq_server {
 // Plans and enqueues one tick (called without the lock; only the scheduler
 // thread touches slots).  Returns the status of the launch.
 int tsq_server::launch(Slot &s, std::vector<std::shared_ptr<Request>> &&reqs, int64_t bytes) {
+  tsq::TraceRange tr("server tick launch");
   s.reqs = std::move(reqs);
   s.first.clear();
   s.seqbuf.clear();

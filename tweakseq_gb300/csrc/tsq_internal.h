@@ -91,6 +91,7 @@ struct FillArgs {
   const uint8_t *ccodes;  // int16x2 fill: class code per residue (0 for invalid ones), same offsets as codes
   const int8_t *cmatrix;  // int16x2 fill: nclasses x nclasses class scores
   int32_t nclasses;
+  int32_t spin_limit;     // CTA fill: polls per bounded wait (0 = the compiled default)
 };
 
 // Compacts the pairs an int16 CHECK launch flagged into a warp-task list
