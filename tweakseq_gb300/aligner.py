@@ -92,6 +92,16 @@ def pair_table(a_off, a_len, b_off, b_len) -> np.ndarray:
     return t
 
 
+def _per_pair_status(rc: int, raw: np.ndarray) -> bool:
+    """True when a batch call's status is OK or one that pairs of the batch
+    report in their own status field (an invalid residue, a device-side
+    wait that ran out, a pair too large for memory): the results of the
+    other pairs are valid then."""
+    if rc == N.TSQ_OK:
+        return True
+    return rc in (N.E_INVALID_RESIDUE, N.E_TIMEOUT, N.E_TOO_LARGE) and bool((raw["status"] == rc).any())
+
+
 def _collect(raw: np.ndarray, strings: bool) -> BatchResult:
     L = N.lib()
     table = np.empty(len(raw), dtype=[(k, np.int32) for k in
@@ -153,7 +163,7 @@ def align_batch(pairs, matrix="blosum62", gap_open=11, gap_extend=1, mode="globa
     o = _opts(use_graph, autotune, wait_polls=wait_polls)
     rc = L.tsq_align_batch(seqs.ctypes.data if len(seqs) else None, len(seqs), tab.ctypes.data if len(tab) else None,
                            len(tab), ctypes.byref(p), ctypes.byref(o), raw.ctypes.data if len(raw) else None)
-    if rc not in (N.TSQ_OK, N.E_INVALID_RESIDUE):
+    if not _per_pair_status(rc, raw):
         N.check(rc, "tsq_align_batch")
     res = _collect(raw, output == "alignment" or output == 2)
     del keep
@@ -195,7 +205,7 @@ class Batch:
     def results(self, check=True) -> BatchResult:
         raw = np.zeros(self.n, dtype=N.RESULT_DTYPE)
         rc = N.lib().tsq_batch_results(self._h, raw.ctypes.data if self.n else None)
-        if rc not in (N.TSQ_OK, N.E_INVALID_RESIDUE):
+        if not _per_pair_status(rc, raw):
             N.check(rc, "tsq_batch_results")
         res = _collect(raw, self.output in ("alignment", 2))
         if check and rc != N.TSQ_OK:
