@@ -40,7 +40,7 @@ int occupancy_i16(bool check, bool local, size_t smem) {
 }
 
 size_t smem_i16(int nclasses) {
-  return size_t(kMatBytes) + size_t(2 * nclasses) * kThreads16 * sizeof(uint2) +
+  return size_t(kMatBytes16) + size_t(2 * nclasses) * kThreads16 * sizeof(uint2) +
          size_t(kSlots16) * (kTopRing * sizeof(uint32_t) + kCodeRing16 + 2 * kRingPad);
 }
 

@@ -56,6 +56,11 @@ constexpr int32_t kNeg16 = -32000;
 constexpr int32_t kBias16 = 32768;
 constexpr uint32_t kBias2 = 0x80008000u;  // value 0 in both (biased) halves
 constexpr uint32_t kNeg2 = 0x03000300u;   // kNeg16 in both (biased) halves
+// The class matrix is staged with one 32-byte row per class, plus a row of
+// zeros that padding rows (past the end of a) read, so that a lane's
+// profile is built from whole rows (four classes per word).
+constexpr int kMatRow16 = 32;
+constexpr int kMatBytes16 = (kLetters + 1) * kMatRow16 + 32;  // 896, a 64-byte multiple
 
 __device__ __forceinline__ uint32_t pack2(int32_t lo, int32_t hi) {
   return (uint32_t(lo) & 0xFFFFu) | (uint32_t(hi) << 16);
@@ -97,6 +102,46 @@ __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
   return d;
 }
 
+
+// 4x4 byte transpose: w[i] holds bytes (x_i0, x_i1, x_i2, x_i3); o[k]
+// receives (x_0k, x_1k, x_2k, x_3k).
+__device__ __forceinline__ void transpose4x4(const uint32_t w0, const uint32_t w1, const uint32_t w2,
+                                             const uint32_t w3, uint32_t o[4]) {
+  const uint32_t t0 = prmt(w0, w1, 0x5140u), t1 = prmt(w2, w3, 0x5140u);
+  const uint32_t t2 = prmt(w0, w1, 0x7362u), t3 = prmt(w2, w3, 0x7362u);
+  o[0] = prmt(t0, t1, 0x5410u);
+  o[1] = prmt(t0, t1, 0x7632u);
+  o[2] = prmt(t2, t3, 0x5410u);
+  o[3] = prmt(t2, t3, 0x7632u);
+}
+
+// True when any of the len letter codes at p is invalid (>= kLetters).  The
+// lanes of a group read the 16-byte aligned chunks covering the range, four
+// loads in flight per lane; bytes of a chunk outside the range are masked
+// off.  The codes buffer is padded past its end, so the last chunk is in
+// bounds.
+__device__ __forceinline__ bool range_has_bad(const uint8_t *p, int len, int t, int G) {
+  if (len <= 0) return false;
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  const uintptr_t a0 = a & ~uintptr_t(15);
+  const int head = int(a - a0);
+  const int nch = (head + len + 15) >> 4;
+  uint32_t any = 0;
+#pragma unroll 4
+  for (int c = t; c < nch; c += G) {
+    const uint4 w = *reinterpret_cast<const uint4 *>(a0 + 16 * uintptr_t(c));
+    const int s = head - 16 * c, e = head + len - 16 * c;  // bytes [s, e) of this chunk are in range
+    const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int lo = min(max(s - 4 * q, 0), 4), hi = min(max(e - 4 * q, 0), 4);
+      const uint32_t mlo = lo >= 4 ? 0u : (0xFFFFFFFFu << (8 * lo));
+      const uint32_t mhi = hi >= 4 ? 0xFFFFFFFFu : ((1u << (8 * hi)) - 1u);
+      any |= __vcmpgeu4(ww[q], 0x1A1A1A1Au) & mlo & mhi;
+    }
+  }
+  return any != 0;
+}
 
 // The lane width G is a run-time value: one code path serves every width,
 // which keeps the kernel small enough for the instruction cache.
@@ -145,8 +190,7 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
   bool bad = false;
   if (have) {
     const uint8_t *la = A.codes + A.pairs[pid].a_off, *lb = A.codes + boff;
-    for (int k = t; k < m; k += G) bad |= la[k] >= kLetters;
-    for (int k = t; k < n; k += G) bad |= lb[k] >= kLetters;
+    bad = range_has_bad(la, m, t, G) || range_has_bad(lb, n, t, G);
   }
   const unsigned gm = group_mask_rt(lane, G);
   const bool gbad = (__ballot_sync(0xffffffffu, bad) & gm) != 0;
@@ -174,31 +218,37 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
     const int nact = gact ? n : 0;
     const int rowA = pass * P2 + t * R;  // band A rows rowA+1 .. rowA+R (1-based)
     const int rowB = rowA + P;           // band B rows rowB+1 .. rowB+R
-    // Profile of this lane's 16 rows (padding rows score 0).
+    // Profile of this lane's 16 rows (padding rows read the zero row and
+    // score 0): each row's class row is read four classes per word and the
+    // words of four rows are transposed into per-class words.
     {
-      int qa[R], qb[R];
+      int xa[R], xb[R];  // byte offsets of the rows' class rows in s_mat
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        qa[r] = (gact && rowA + r < m) ? int(qa_codes[rowA + r]) : -1;
-        qb[r] = (gact && rowB + r < m) ? int(qa_codes[rowB + r]) : -1;
+        xa[r] = kMatRow16 * ((gact && rowA + r < m) ? int(qa_codes[rowA + r]) : ncls);
+        xb[r] = kMatRow16 * ((gact && rowB + r < m) ? int(qa_codes[rowB + r]) : ncls);
       }
-#pragma unroll 2
-      for (int c = 0; c < ncls; ++c) {
-        uint32_t wa[2], wb[2];
+#pragma unroll 1
+      for (int cb = 0; cb < ncls; cb += 4) {
+        uint32_t a[R], b[R];
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          uint32_t va = 0, vb = 0;
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            const int xa = qa[q * 4 + k], xb = qb[q * 4 + k];
-            va |= (xa >= 0 ? uint32_t(uint8_t(s_mat[xa * ncls + c])) : 0u) << (8 * k);
-            vb |= (xb >= 0 ? uint32_t(uint8_t(s_mat[xb * ncls + c])) : 0u) << (8 * k);
-          }
-          wa[q] = va;
-          wb[q] = vb;
+        for (int r = 0; r < R; ++r) {
+          a[r] = *reinterpret_cast<const uint32_t *>(s_mat + xa[r] + cb);
+          b[r] = *reinterpret_cast<const uint32_t *>(s_mat + xb[r] + cb);
         }
-        s_prof[(2 * c) * kThreads16 + threadIdx.x] = make_uint2(wa[0], wa[1]);
-        s_prof[(2 * c + 1) * kThreads16 + threadIdx.x] = make_uint2(wb[0], wb[1]);
+        uint32_t a0[4], a1[4], b0[4], b1[4];
+        transpose4x4(a[0], a[1], a[2], a[3], a0);
+        transpose4x4(a[4], a[5], a[6], a[7], a1);
+        transpose4x4(b[0], b[1], b[2], b[3], b0);
+        transpose4x4(b[4], b[5], b[6], b[7], b1);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int c = cb + k;
+          if (c < ncls) {
+            s_prof[(2 * c) * kThreads16 + threadIdx.x] = make_uint2(a0[k], a1[k]);
+            s_prof[(2 * c + 1) * kThreads16 + threadIdx.x] = make_uint2(b0[k], b1[k]);
+          }
+        }
       }
     }
 
@@ -234,27 +284,33 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       tv[0] = top_ring[0];
     }
 
-    // Steps run in pairs; an odd count gets one padding step, in which every
-    // lane's columns are out of range (s - t >= n + G).  Steps [2G, n_min)
-    // -- n_min the shortest column count of the warp's groups this pass,
-    // 0 when one of them is idle -- have both halves of every lane in range:
-    // they run without range tests or masks.
+    // Steps run in units of two (the ramps) or four (the interior); an odd
+    // count gets one padding step, in which every lane's columns are out of
+    // range (s - t >= n + G).  Steps [2G, n_min) -- n_min the shortest
+    // column count of the warp's groups this pass, 0 when one of them is
+    // idle -- have both halves of every lane in range: they run without
+    // range tests or masks, four per unit.
     const int steps_pad = (max_steps + 1) & ~1;
     int n_min = nact;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) n_min = min(n_min, __shfl_xor_sync(0xffffffffu, n_min, o));
-    const int i0 = min(2 * G, steps_pad);
-    const int i1 = max(i0, n_min & ~1);
+    const int i0 = min(2 * G, steps_pad);  // a multiple of 4 whenever the interior is not empty
+    const int i1 = max(i0, n_min & ~3);
 
-    // Ring indexes of a step pair: the odd step reads one entry further,
-    // into the mirrored head past the ring's end when the even one is last.
+    // Ring positions of a unit's first step: step k of the unit reads k
+    // entries further, into the mirrored head past the ring's end when the
+    // unit starts near it (the mirrors hold 16 bytes: 16 codes, 4 top-row
+    // entries), so a unit computes its ring addresses once.
     const int cA0 = int(boff & (kCodeRing16 - 1)) - t + 1 + kCodeRing16;  // code of column jA + 1, positive
     const int cB0 = cA0 - G;                                               // code of column jB + 1
-    auto step = [&](const int s, auto k_tag, auto interior_tag, const int ia, const int ib, const int it) {
+    auto step = [&](const int s, auto k_tag, auto interior_tag, auto last_tag, const uint8_t *codeA,
+                    const uint8_t *codeB, const uint32_t *topp) {
       constexpr int k = decltype(k_tag)::value;
+      constexpr int cur = k & 1, nxt = cur ^ 1;
       constexpr bool INTERIOR = decltype(interior_tag)::value;
-      // Chunk boundaries fall on odd steps only (pairs start on even steps).
-      if (k == 1 && ((s + 1) & (kChunk - 1)) == 0) {
+      // Chunk boundaries fall on the last step of a unit only (units start
+      // on steps that are multiples of their size).
+      if (decltype(last_tag)::value && ((s + 1) & (kChunk - 1)) == 0) {
         cp_async_wait_all();
         __syncwarp();
         stage_chunk_rt<uint32_t, kCodeRing16>(G, (s + 1) / kChunk + 1, t, nact, top, top_ring, A.ccodes, boff,
@@ -264,20 +320,20 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       const uint32_t rH = __shfl_sync(0xffffffffu, outH, src_lane);
       const uint32_t rF = __shfl_sync(0xffffffffu, outF, src_lane);
       const int jA = s - t, jB = jA - G;
-      const uint2 wa = pa[k], wb = pb[k];
+      const uint2 wa = pa[cur], wb = pb[cur];
       {
-        const int ca = code_ring[ia];
-        const int cb = code_ring[ib];
-        pa[k ^ 1] = profA[(2 * ca) * kThreads16];
-        pb[k ^ 1] = profB[(2 * cb) * kThreads16];
+        const int ca = codeA[k];
+        const int cb = codeB[k];
+        pa[nxt] = profA[(2 * ca) * kThreads16];
+        pb[nxt] = profB[(2 * cb) * kThreads16];
       }
       // Lane 0: band A from the staged top row, band B from lane G-1's
       // band-A bottom; other lanes take the shuffled values whole.  Lane-
       // dependent PRMT selectors instead of a branch; every lane of a group
       // reads lane 0's ring entry (one broadcast address per group).
-      const uint32_t upH = prmt(tv[k], rH, selH);
-      const uint32_t upF = prmt(tv[k], rF, selF);
-      tv[k ^ 1] = top_ring[it];
+      const uint32_t upH = prmt(tv[cur], rH, selH);
+      const uint32_t upF = prmt(tv[cur], rF, selF);
+      tv[nxt] = topp[k];
       const bool vA = INTERIOR || (unsigned)jA < (unsigned)nact;
       const bool vB = INTERIOR || (unsigned)jB < (unsigned)nact;
       if (vA || vB) {
@@ -338,15 +394,25 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       }
     };
     int s0 = 0;
-    auto pair_of_steps = [&](auto interior_tag) {
-      const int ia = (cA0 + s0) & (kCodeRing16 - 1), ib = (cB0 + s0) & (kCodeRing16 - 1);
-      const int it = (s0 + 1) & (kTopRing - 1);
-      step(s0, IntTag<0>{}, interior_tag, ia, ib, it);
-      step(s0 + 1, IntTag<1>{}, interior_tag, ia + 1, ib + 1, it + 1);
+    auto pair_of_steps = [&]() {
+      const uint8_t *codeA = code_ring + ((cA0 + s0) & (kCodeRing16 - 1));
+      const uint8_t *codeB = code_ring + ((cB0 + s0) & (kCodeRing16 - 1));
+      const uint32_t *topp = top_ring + ((s0 + 1) & (kTopRing - 1));
+      step(s0, IntTag<0>{}, BoolTag<false>{}, BoolTag<false>{}, codeA, codeB, topp);
+      step(s0 + 1, IntTag<1>{}, BoolTag<false>{}, BoolTag<true>{}, codeA, codeB, topp);
     };
-    for (; s0 < i0; s0 += 2) pair_of_steps(BoolTag<false>{});
-    for (; s0 < i1; s0 += 2) pair_of_steps(BoolTag<true>{});
-    for (; s0 < steps_pad; s0 += 2) pair_of_steps(BoolTag<false>{});
+    auto quad_of_steps = [&]() {
+      const uint8_t *codeA = code_ring + ((cA0 + s0) & (kCodeRing16 - 1));
+      const uint8_t *codeB = code_ring + ((cB0 + s0) & (kCodeRing16 - 1));
+      const uint32_t *topp = top_ring + ((s0 + 1) & (kTopRing - 1));
+      step(s0, IntTag<0>{}, BoolTag<true>{}, BoolTag<false>{}, codeA, codeB, topp);
+      step(s0 + 1, IntTag<1>{}, BoolTag<true>{}, BoolTag<false>{}, codeA, codeB, topp);
+      step(s0 + 2, IntTag<2>{}, BoolTag<true>{}, BoolTag<false>{}, codeA, codeB, topp);
+      step(s0 + 3, IntTag<3>{}, BoolTag<true>{}, BoolTag<true>{}, codeA, codeB, topp);
+    };
+    for (; s0 < i0; s0 += 2) pair_of_steps();
+    for (; s0 < i1; s0 += 4) quad_of_steps();
+    for (; s0 < steps_pad; s0 += 2) pair_of_steps();
     cp_async_wait_all();
     __syncwarp();
 
@@ -426,10 +492,15 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
 template <bool LOCAL, bool CHECK>
 __global__ void __launch_bounds__(kThreads16) fill_i16_kernel(const FillArgs A) {
   extern __shared__ __align__(16) uint8_t smem[];
-  int8_t *s_mat = reinterpret_cast<int8_t *>(smem);  // class scores, nclasses x nclasses
-  uint2 *s_prof = reinterpret_cast<uint2 *>(smem + kMatBytes);
-  uint8_t *s_rings = smem + kMatBytes + size_t(2 * A.nclasses) * kThreads16 * sizeof(uint2);
-  for (int k = threadIdx.x; k < A.nclasses * A.nclasses; k += blockDim.x) s_mat[k] = A.cmatrix[k];
+  // Class scores, one 32-byte row per class, then a zero row (index
+  // nclasses) for padding rows.
+  int8_t *s_mat = reinterpret_cast<int8_t *>(smem);
+  uint2 *s_prof = reinterpret_cast<uint2 *>(smem + kMatBytes16);
+  uint8_t *s_rings = smem + kMatBytes16 + size_t(2 * A.nclasses) * kThreads16 * sizeof(uint2);
+  for (int k = threadIdx.x; k < kMatBytes16; k += blockDim.x) {
+    const int x = k / kMatRow16, c = k % kMatRow16;
+    s_mat[k] = (x < A.nclasses && c < A.nclasses) ? A.cmatrix[x * A.nclasses + c] : int8_t(0);
+  }
   // Code rings start as class 0: a group without a pair still reads its
   // ring, and the step uses what it reads as a profile index unchecked
   // (every class code the rings receive is below nclasses).
