@@ -152,6 +152,38 @@ class ClockSampler:
                 "samples": len(sms)}
 
 
+def hbm_peak():
+    """Measured HBM copy bandwidth (GB/s) and where it came from."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        try:
+            return float(json.load(open(path))["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+        except (OSError, ValueError, KeyError):
+            pass
+    return 6800.0, "fallback 6.8 TB/s (no measured peak on this box)"
+
+
+_DPX = {}
+
+
+def dpx_cell_peak(packed):
+    """Roofline peak of a fill in Gcell/s: the measured DPX-class instruction
+    rate (tsq_probe_dpx) x lanes per instruction / 4 instructions per cell."""
+    from tweakseq_gb300 import aligner as A
+    if packed not in _DPX:
+        _DPX[packed] = A.probe_dpx(packed=packed)
+    return _DPX[packed] * (2.0 if packed else 1.0) / 4.0 / 1e9
+
+
+def traffic_record(name):
+    """The ncu record committed as profiles/<name>.json (or None)."""
+    path = os.path.join(ROOT, "profiles", name + ".json")
+    try:
+        return json.load(open(path))
+    except (OSError, ValueError):
+        return None
+
+
 def traffic_from_profile(name="fill_uneven_pairs_100k"):
     """DRAM bytes (read + write) per launch of a kernel, from the ncu record
     committed as profiles/<name>.json (or None when there is none)."""
@@ -318,8 +350,7 @@ def run_ours(args):
     # Roofline denominator: the measured int16x2 DPX instruction rate, two
     # cells per instruction, 4 DPX-class instructions per cell (E add-max, F
     # add-max, diagonal add, three-way max).
-    dpx_rate = A.probe_dpx(packed=True)     # int16x2 DPX instructions / lane / s
-    peak_gcups = dpx_rate * 2.0 / 4.0 / 1e9
+    peak_gcups = dpx_cell_peak(True)
     fill_avg_ms = float(np.mean(fill_ms))
     achieved = cells / (fill_avg_ms * 1e-3) / 1e9
     roofline = {"bound": "int", "achieved": achieved, "peak": peak_gcups, "unit": "Gcell/s",
@@ -523,6 +554,7 @@ def configs_leg(c3_pairs=12):
                    f"and {c3_pairs - 1} seeded) byte for byte: score, coordinates, identity, both gapped strings",
         "oracle": {"threads": nthr, "seconds": oracle_s}}
     del res
+    out["long_dna_pairs_1000"]["kernels"] = long_pair_kernels(ps)
     # The guide-tree all-vs-all in full.
     ps = W.guide_tree_families()
     with A.Batch(ps, output="identity", use_graph=True) as b:
@@ -534,11 +566,72 @@ def configs_leg(c3_pairs=12):
     sub = ps.subset(idx)
     want = O.batch(sub.seqs, sub.a_off, sub.a_len, sub.b_off, sub.b_len, mode=O.MODE_IDENT, nthreads=cores)
     mism = int(sum((res.table[f][idx] != want[f]).sum() for f in ("score", "n_ident", "n_cols")))
+    fill_gcups = ps.cells / (st["fill_ms"] * 1e-3) / 1e9
+    peak = dpx_cell_peak(False)
+    rec = traffic_record("fill_i32_identity_guide_tree_200k")
+    traffic = rec["dram_bytes_per_launch"] * len(ps) / rec["pairs"] if rec else None
+    # The plain per-pair path on a sample of the same pairs.
+    plain_idx = np.random.default_rng(6).choice(len(ps), 300, replace=False)
+    t0 = time.perf_counter()
+    for k in plain_idx:
+        a, bb = ps.pair(int(k))
+        A.align_pair(a, bb, output="identity")
+    plain_s = time.perf_counter() - t0
+    plain_cells = float(np.dot(ps.a_len[plain_idx].astype(np.int64), ps.b_len[plain_idx].astype(np.int64)))
     out["guide_tree_all_vs_all"] = {
         "pairs": len(ps), "cells": ps.cells, "output": "score + identity (global, BLOSUM62 11/1)",
-        "batched_gcups": ps.cells / (st["device_ms"] * 1e-3) / 1e9, "fill_gcups": ps.cells / (st["fill_ms"] * 1e-3) / 1e9,
+        "batched_gcups": ps.cells / (st["device_ms"] * 1e-3) / 1e9, "fill_gcups": fill_gcups,
+        "plain_gcups": plain_cells / plain_s / 1e9, "plain_pairs": len(plain_idx),
+        "roofline": {"bound": "int", "kernel": "fill_i32_kernel (identity, global)", "achieved": fill_gcups,
+                     "peak": peak, "unit": "Gcell/s", "frac": fill_gcups / peak, "traffic": traffic,
+                     "traffic_source": "ncu DRAM bytes of a 200,000-pair launch, scaled by pairs",
+                     "peak_source": "measured live: tsq_probe_dpx int32 rate / 4 DPX instructions per cell"},
         "mismatches_vs_oracle": mism, "checked": "4,000 seeded pairs"}
     return out
+
+
+def long_pair_kernels(ps, n_pairs=152):
+    """Rooflines of the long-pair kernels: a device-resident batch of the
+    first n_pairs long DNA pairs (one CTA per pair: the CTA traceback fill,
+    then one walker warp per pair), timed by the batch's own events."""
+    from tweakseq_gb300 import aligner as A
+    sub = ps.subset(np.arange(n_pairs))
+    fills, rest = [], []
+    with A.Batch(sub, matrix="dna", gap_open=5, gap_extend=2, output="alignment", use_graph=False) as b:
+        b.run()
+        for _ in range(3):
+            b.run()
+            st = b.stats()
+            fills.append(st["fill_ms"])
+            rest.append(st["device_ms"] - st["fill_ms"])
+        res = b.results()
+    fill_s = float(np.median(fills)) * 1e-3
+    walk_s = float(np.median(rest)) * 1e-3
+    gc = sub.cells / fill_s / 1e9
+    peak = dpx_cell_peak(False)
+    hbm, hbm_src = hbm_peak()
+    rec = traffic_record("fill_cta_long_dna_32")
+    traffic = rec["dram_bytes_per_launch"] * sub.cells / rec["cells"] if rec else None
+    plane_gbs = 0.5 * sub.cells / fill_s / 1e9
+    # Walker bytes: the nibble of each walked cell, both gapped rows written
+    # and the residues read.
+    cols = res.table["n_cols"].astype(np.float64)
+    walk_bytes = float((0.5 * cols + 2 * cols).sum() + sub.a_len.sum() + sub.b_len.sum())
+    return {
+        "pairs": n_pairs, "cells": sub.cells,
+        "fill_cta_kernel": {
+            "fill_ms": fill_s * 1e3,
+            "roofline": {"bound": "int", "achieved": gc, "peak": peak, "unit": "Gcell/s", "frac": gc / peak,
+                         "traffic": traffic, "traffic_source": "ncu DRAM bytes of a 32-pair launch, scaled by cells",
+                         "peak_source": "measured live: tsq_probe_dpx int32 rate / 4 DPX instructions per cell"},
+            "plane_writes": {"bound": "hbm", "achieved": plane_gbs, "peak": hbm, "unit": "GB/s",
+                             "frac": plane_gbs / hbm, "bytes_per_cell": 0.5, "peak_source": hbm_src}},
+        "walk_warp_kernel": {
+            "ms": walk_s * 1e3, "note": "device time after the fill: the walker and the result copies",
+            "roofline": {"bound": "latency", "achieved": walk_bytes / walk_s / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": walk_bytes / walk_s / 1e9 / hbm, "bytes": walk_bytes,
+                         "bytes_note": "0.5 B per walked cell + 2 B of gapped rows per column + the residues",
+                         "peak_source": hbm_src}}}
 
 
 def msa_leg(cpu_cols=40, cpu_tree_leaves=1000):
@@ -556,8 +649,7 @@ def msa_leg(cpu_cols=40, cpu_tree_leaves=1000):
 
     out = {}
     L = N.lib()
-    peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"] if os.path.exists(
-        os.path.join(ROOT, "MEASURED_PEAKS.json")) else 6800.0
+    peak, _ = hbm_peak()
     for nseq, ncols in ((4000, 1000), (100_000, 2000)):
         rng = np.random.default_rng(nseq)
         # Columns with a favourite residue (kept in 60 % of rows), 15 % gaps.
