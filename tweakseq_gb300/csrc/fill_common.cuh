@@ -42,6 +42,15 @@ __device__ __forceinline__ int32_t sbyte_dyn(uint32_t w, int k) {
   }
 }
 
+// max(a, b) and whether a won (a >= b, so a wins ties): one compare and one
+// select.  (The predicated DPX max, __vibmax_s32, costs four instructions --
+// three on the ALU pipe -- on sm_103a.)
+__device__ __forceinline__ int32_t max_pred(int32_t a, int32_t b, bool *a_won) {
+  const bool p = a >= b;
+  *a_won = p;
+  return p ? a : b;
+}
+
 // Global-mode boundary value H(i,0) = H(0,i) = -(open + i*ext), H(0,0) = 0.
 __device__ __forceinline__ int32_t edge_h(int i, int32_t go, int32_t ge, bool local) {
   return (local || i == 0) ? 0 : -(go + i * ge);

@@ -301,11 +301,11 @@ __global__ void __launch_bounds__(kCtaThreads, 1) fill_cta_kernel(const FillArgs
 #pragma unroll
           for (int r = 0; r < R; ++r) {
             const int32_t sc = sbyte_dyn(r < 4 ? pcur.x : pcur.y, r);
-            // E and F: opening beats extending on ties (one DPX max with its
-            // predicate each).
+            // E and F: opening beats extending on ties (a max that also reports
+            // which operand won, max_pred).
             bool eopen, fopen;
-            const int32_t e = __vibmax_s32(H[r] - oe, E[r] - ge, &eopen);
-            const int32_t f = __vibmax_s32(hu - oe, fv - ge, &fopen);
+            const int32_t e = max_pred(H[r] - oe, E[r] - ge, &eopen);
+            const int32_t f = max_pred(hu - oe, fv - ge, &fopen);
             const int32_t dd = d + sc;
             int32_t h;
             if constexpr (OUT == kOutScore) {
@@ -320,8 +320,8 @@ __global__ void __launch_bounds__(kCtaThreads, 1) fill_cta_kernel(const FillArgs
               // H: diagonal beats E beats F on ties: pde = (diag >= E),
               // pxf = (max(diag, E) >= F).
               bool pde, pxf;
-              const int32_t x = __vibmax_s32(dd, e, &pde);
-              h = __vibmax_s32(x, f, &pxf);
+              const int32_t x = max_pred(dd, e, &pde);
+              h = max_pred(x, f, &pxf);
               int dir = pxf ? (pde ? int(kDirDiag) : int(kDirE)) : int(kDirF);
               if (LOCAL && h <= 0) {
                 h = 0;
