@@ -62,7 +62,7 @@ def parse_args():
     ap.add_argument("--no-configs", action="store_true", help="skip the other configurations")
     ap.add_argument("--configs-only", action="store_true", help="run only the other configurations")
     ap.add_argument("--msa-only", action="store_true", help="run only the consensus and guide-tree legs")
-    ap.add_argument("--profile-case", choices=["long_dna", "identity", "consensus"], default=None,
+    ap.add_argument("--profile-case", choices=["long_dna", "identity", "consensus", "uniform"], default=None,
                     help="small profiling case of another kernel (for ncu)")
     return ap.parse_args()
 
@@ -732,7 +732,9 @@ def run_profile_case(args):
     long_dna (32 DNA pairs of 10-12 kb with traceback: the CTA fill and the
     walker),
     identity (200,000 pairs of the guide-tree all-vs-all: the int32 identity
-    fill), consensus (100,000 x 2,000 alignment: the class-count kernel).
+    fill), consensus (100,000 x 2,000 alignment: the class-count kernel),
+    uniform (20,000 protein pairs of 320 x 2,000: the int16x2 score fill with
+    interior steps only, for instruction counts per step).
     Device-resident, no graph, warm-up then timed runs."""
     import torch
 
@@ -743,10 +745,20 @@ def run_profile_case(args):
 
     B.build()
     case = args.profile_case
-    if case in ("long_dna", "identity"):
+    if case in ("long_dna", "identity", "uniform"):
         if case == "long_dna":
             ps = W.long_dna_pairs(32, lo=10_000, hi=12_000)
             kw = dict(matrix="dna", gap_open=5, gap_extend=2, output="alignment")
+        elif case == "uniform":
+            # Equal shapes, so nearly every step of the int16x2 fill is an
+            # interior step: instruction counts per step read off directly.
+            rng = np.random.default_rng(1)
+            seqs, pairs = [], []
+            for k in range(20000):
+                seqs += [W.random_protein(rng, 320).tobytes(), W.random_protein(rng, 2000).tobytes()]
+                pairs.append((2 * k, 2 * k + 1))
+            ps = W._pairset_from_lists(seqs, pairs)
+            kw = dict(output="score")
         else:
             ps = W.guide_tree_families()
             ps = ps.subset(np.arange(200_000))
