@@ -555,9 +555,21 @@ def configs_leg(c3_pairs=12):
         "oracle": {"threads": nthr, "seconds": oracle_s}}
     del res
     out["long_dna_pairs_1000"]["kernels"] = long_pair_kernels(ps)
-    # The guide-tree all-vs-all in full.
+    # The guide-tree all-vs-all in full, with autotuned length buckets (a
+    # quick tuning pass on this GPU first) and, for comparison, without.
     ps = W.guide_tree_families()
+    import tempfile
+    tune_path = os.path.join(tempfile.mkdtemp(), "tune.json")
+    t0 = time.perf_counter()
+    A.tune(tune_path, quick=True)
+    tune_s = time.perf_counter() - t0
+    A.load_tuning(tune_path)
+    tuned_entries = [e for e in json.load(open(tune_path))["entries"] if e["out"] == "identity"]
     with A.Batch(ps, output="identity", use_graph=True) as b:
+        b.run()
+        b.run()
+        st_untuned = b.stats()
+    with A.Batch(ps, output="identity", use_graph=True, autotune=True) as b:
         b.run()
         b.run()
         st = b.stats()
@@ -582,6 +594,8 @@ def configs_leg(c3_pairs=12):
         "pairs": len(ps), "cells": ps.cells, "output": "score + identity (global, BLOSUM62 11/1)",
         "batched_gcups": ps.cells / (st["device_ms"] * 1e-3) / 1e9, "fill_gcups": fill_gcups,
         "plain_gcups": plain_cells / plain_s / 1e9, "plain_pairs": len(plain_idx),
+        "autotune": {"tune_s": tune_s, "identity_buckets": tuned_entries,
+                     "untuned_fill_gcups": ps.cells / (st_untuned["fill_ms"] * 1e-3) / 1e9},
         "roofline": {"bound": "int", "kernel": "fill_i32_kernel (identity, global)", "achieved": fill_gcups,
                      "peak": peak, "unit": "Gcell/s", "frac": fill_gcups / peak, "traffic": traffic,
                      "traffic_source": "ncu DRAM bytes of a 200,000-pair launch, scaled by pairs",

@@ -296,9 +296,11 @@ Shape ShapeChooser::pick(int m, int n, int rows_per_lane) const {
   }
   const int rows_cap = pow2ceil((m + rows_per_lane - 1) / rows_per_lane);
   int G = std::max(g_occ, g_lat);
+  if (force.shape) return force.sh;
   Shape sh{};
-  if (use_table && tune_table_pick(out_mode, m, n, &sh) && shape_supported(sh, out_mode, local)) {
-    if (tune_forced()) return sh;
+  TunedChoice tc;
+  if (use_table && tune_table_pick(out_mode, m, n, &tc) && shape_supported(Shape{tc.sh.G, tc.sh.R, 0}, out_mode, local)) {
+    sh = tc.sh;
     G = std::max(G, sh.G);
   } else {
     sh.R = kR;
@@ -598,6 +600,7 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
     ch.avg_lane_steps = double(shape_cells) / (lanes * kR);
   }
   ch.use_table = b->autotune && tune_table_loaded();
+  ch.force = b->tune_force;
   PlanScratch &ps = b->scratch;
   ps.lsel.resize(size_t(n));
   ps.gsel.resize(size_t(n));
@@ -634,15 +637,19 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
       for (int64_t k = lo; k < hi; ++k) {
         const PairDev &pd = b->pairs_h[size_t(k)];
         int8_t lt = 0;
-        if (try16) {
+        // A tuned table may prefer int32 over int16x2 for this length bucket,
+        // or the CTA fill for its int32 pairs.
+        TunedChoice tc;
+        const bool tuned = ch.use_table && !ch.force.shape && tune_table_pick(b->out_mode, pd.a_len, pd.b_len, &tc);
+        if (try16 && !(tuned && tc.sh.i16 == 0)) {
           const int64_t lowest = 3 * go + (int64_t(pd.a_len) + 512 + pd.b_len + 1) * ge + go + ge + 128 + sneg;
           const bool lower_ok = lowest + go + ge < 31000 && ge <= 700 && pd.b_len <= 65535;
           const bool upper_ok = smax * std::min(pd.a_len, pd.b_len) + smax < 32767;
           if (lower_ok) lt = (upper_ok && p->lane == TSQ_LANE_AUTO) ? 1 : 2;
         }
-        if (lt == 0) {
+        if (lt == 0 && pd.a_len > 0 && pd.b_len > 0) {
           const double steps32 = double((pd.a_len + 255) / 256) * double(pd.b_len + 31);
-          if (pd.a_len > 0 && pd.b_len > 0 && steps32 > cta_budget) lt = 3;
+          if (steps32 > cta_budget || ch.force.cta || (tuned && tc.cta)) lt = 3;
         }
         lsel[size_t(k)] = lt;
         sp.n_checked += lt == 2;

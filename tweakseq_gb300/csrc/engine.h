@@ -61,6 +61,23 @@ struct Launch {
   int64_t bnd_offset = 0;  // bytes into the boundary scratch
 };
 
+// What the autotuner forces while it times one candidate: a lane width for
+// every pair, and (cta) the CTA fill for every int32 pair.  Carried by the
+// batch object into its plan, so the planner's worker threads see it.
+struct TuneForce {
+  bool shape = false;
+  Shape sh{};
+  bool cta = false;
+};
+
+// A tuned table's choice for a length bucket: lane width, lane type (i16: 1
+// int16x2 where its range is proven or checked, 0 int32) and whether int32
+// pairs take the CTA fill.
+struct TunedChoice {
+  Shape sh{};
+  int cta = 0;
+};
+
 // Kernel-shape choice.  A tuned table (lengths -> shape) overrides the
 // occupancy heuristic when loaded and enabled.
 struct ShapeChooser {
@@ -72,6 +89,7 @@ struct ShapeChooser {
   // more than about half of it, or it becomes the batch's tail.
   double avg_lane_steps = 0.0;
   bool use_table = false;
+  TuneForce force;
   Shape pick(int m, int n, int rows_per_lane) const;
 };
 
@@ -95,8 +113,7 @@ struct PlanScratch {
 };
 
 bool tune_table_loaded();
-bool tune_forced();
-bool tune_table_pick(int out_mode, int m, int n, Shape *sh);
+bool tune_table_pick(int out_mode, int m, int n, TunedChoice *c);
 
 }  // namespace tsq
 
@@ -117,6 +134,7 @@ struct tsq_batch {
   bool use_graph = false;
   bool autotune = false;
   int32_t wait_polls = 0;  // CTA fill: polls per bounded wait (0 = default)
+  tsq::TuneForce tune_force;  // set by the autotuner for the next plan
   int64_t n = 0;
   int64_t seqs_len = 0;
   int64_t cells = 0;

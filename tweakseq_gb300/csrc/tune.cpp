@@ -1,12 +1,20 @@
 // tune.cpp -- the length-bucket autotuner.
 //
 // For each output kind (score, identity, alignment) and each length bucket
-// (by the longer sequence of a pair), tsq_tune_run times every compiled
-// kernel shape on seeded synthetic protein pairs that fill the GPU and keeps
-// the fastest in cells per second.  The table is written as JSON and read
-// back by tsq_tune_load; batches created with opts.autotune consult it.
-// Few-pair batches still get at least enough lanes per pair to keep every
-// SM busy (the planner takes the larger of the tuned and the occupancy G).
+// (by the longer sequence of a pair), tsq_tune_run times the candidates on
+// seeded synthetic protein pairs that fill the GPU and keeps the fastest in
+// cells per second:
+//   - the lane width G (4, 8, 16 or 32 lanes per pair);
+//   - for score output, the lane type: int16x2 (proven or overflow-checked
+//     with the exact int32 re-run) against int32;
+//   - for buckets of 1,024 residues and more, the CTA fill (one pair per
+//     8-warp CTA, the pair's bands striped over the warps) against one pair
+//     per warp group.
+// The table is written as JSON and read back by tsq_tune_load; batches
+// created with opts.autotune consult it.  Few-pair batches still get at
+// least enough lanes per pair to keep every SM busy (the planner takes the
+// larger of the tuned and the occupancy G), and a pair too long for any
+// warp group keeps the CTA fill whatever the table says.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -23,7 +31,8 @@ namespace {
 
 struct Entry {
   int out, lo, hi;
-  Shape sh;
+  Shape sh;  // G, R, and i16 (1: int16x2 lanes where their range allows, 0: int32)
+  int cta;   // 1: int32 pairs of the bucket take the CTA fill
   double gcups;
 };
 
@@ -33,10 +42,9 @@ bool g_loaded = false;
 
 constexpr int kEdges[] = {0, 64, 128, 256, 512, 1024, 2048, 4096, 8192, 1 << 21};
 constexpr int kNumBuckets = int(sizeof(kEdges) / sizeof(kEdges[0])) - 1;
-constexpr Shape kCandidates[] = {{4, 8, 0}, {8, 8, 0}, {16, 8, 0}, {32, 8, 0}};
+constexpr int kWidths[] = {4, 8, 16, 32};
+constexpr int kCtaFrom = 1024;  // buckets from this length also try the CTA fill
 const char *kOutNames[] = {"score", "identity", "alignment"};
-
-thread_local const Shape *t_force = nullptr;
 
 int find_int(const std::string &obj, const char *key, int *v) {
   const std::string k = std::string("\"") + key + "\"";
@@ -63,23 +71,17 @@ int find_str(const std::string &obj, const char *key, std::string *v) {
 }  // namespace
 
 bool tune_table_loaded() {
-  if (t_force) return true;
   std::lock_guard<std::mutex> g(g_mu);
   return g_loaded;
 }
 
-bool tune_forced() { return t_force != nullptr; }
-
-bool tune_table_pick(int out_mode, int m, int n, Shape *sh) {
-  if (t_force) {
-    *sh = *t_force;
-    return true;
-  }
+bool tune_table_pick(int out_mode, int m, int n, TunedChoice *c) {
   std::lock_guard<std::mutex> g(g_mu);
   const int L = std::max(m, n);
   for (const Entry &e : g_table)
     if (e.out == out_mode && L >= e.lo && L < e.hi) {
-      *sh = e.sh;
+      c->sh = e.sh;
+      c->cta = e.cta;
       return true;
     }
   return false;
@@ -111,10 +113,12 @@ extern "C" int tsq_tune_load(const char *json_path) {
     if (tsq::find_str(obj, "out", &out) || tsq::find_int(obj, "lo", &e.lo) || tsq::find_int(obj, "hi", &e.hi) ||
         tsq::find_int(obj, "G", &e.sh.G) || tsq::find_int(obj, "R", &e.sh.R) || tsq::find_int(obj, "i16", &e.sh.i16))
       return TSQ_E_INVALID_ARG;
+    if (tsq::find_int(obj, "cta", &e.cta)) e.cta = 0;  // tables written before the CTA choice
     e.out = -1;
     for (int k = 0; k < 3; ++k)
       if (out == tsq::kOutNames[k]) e.out = k;
-    if (e.out < 0 || e.lo < 0 || e.hi <= e.lo) return TSQ_E_INVALID_ARG;
+    if (e.out < 0 || e.lo < 0 || e.hi <= e.lo || (e.cta != 0 && e.cta != 1) || (e.sh.i16 != 0 && e.sh.i16 != 1))
+      return TSQ_E_INVALID_ARG;
     if (!tsq::shape_supported(e.sh, e.out, false)) return TSQ_E_INVALID_ARG;
     table.push_back(e);
     pos = b + 1;
@@ -161,27 +165,40 @@ extern "C" int tsq_tune_run(const char *json_path, int32_t quick) {
       p.gap_extend = 1;
       p.mode = TSQ_GLOBAL;
       p.output = out == kOutScore ? TSQ_OUT_SCORE : (out == kOutIdent ? TSQ_OUT_IDENTITY : TSQ_OUT_ALIGNMENT);
-      p.lane = TSQ_LANE_I32;
-      Entry best{out, kEdges[bk], kEdges[bk + 1], Shape{32, 8, 0}, 0.0};
-      for (const Shape &cand : kCandidates) {
-        if (!shape_supported(cand, out, false)) continue;
+      // Candidates: (lane width, lane type, CTA fill).  Each is timed as the
+      // fill time of one planned run (device events), the best of several.
+      struct Cand {
+        int G, i16, cta;
+      };
+      std::vector<Cand> cands;
+      for (int G : kWidths) {
+        cands.push_back(Cand{G, 0, 0});
+        if (out == kOutScore) cands.push_back(Cand{G, 1, 0});
+      }
+      if (kEdges[bk] >= kCtaFrom) cands.push_back(Cand{32, 0, 1});
+      Entry best{out, kEdges[bk], kEdges[bk + 1], Shape{32, 8, 0}, 0, 0.0};
+      for (const Cand &cand : cands) {
         tsq_batch b;
         tsq_batch_opts o{};
         o.device = dev;
-        o.autotune = 1;
-        t_force = &cand;
+        p.lane = cand.i16 ? TSQ_LANE_AUTO : TSQ_LANE_I32;
+        b.tune_force.shape = true;
+        b.tune_force.sh = Shape{cand.G, 8, 0};
+        b.tune_force.cta = cand.cta != 0;
         int rc = batch_plan(&b, seqs.data(), int64_t(seqs.size()), pairs.data(), np, &p, &o, false);
-        t_force = nullptr;
         if (rc) return rc;
         double best_ms = 1e30;
         for (int it = 0; it < (quick ? 3 : 5); ++it) {
           if ((rc = batch_run_async(&b)) || (rc = batch_sync(&b))) return rc;
-          if (it > 0) best_ms = std::min(best_ms, b.stats.fill_ms);
+          // Alignment output: the whole run, since the walker's speed
+          // depends on the plane layout the lane width sets.
+          if (it > 0) best_ms = std::min(best_ms, out == kOutTrace ? b.stats.device_ms : b.stats.fill_ms);
         }
         const double gcups = double(b.cells) / (best_ms * 1e-3) / 1e9;
         if (gcups > best.gcups) {
           best.gcups = gcups;
-          best.sh = cand;
+          best.sh = Shape{cand.G, 8, cand.i16};
+          best.cta = cand.cta;
         }
       }
       table.push_back(best);
@@ -193,8 +210,10 @@ extern "C" int tsq_tune_run(const char *json_path, int32_t quick) {
                prop.minor);
   for (size_t k = 0; k < table.size(); ++k) {
     const Entry &e = table[k];
-    std::fprintf(f, "  {\"out\": \"%s\", \"lo\": %d, \"hi\": %d, \"G\": %d, \"R\": %d, \"i16\": %d, \"gcups\": %.1f}%s\n",
-                 kOutNames[e.out], e.lo, e.hi, e.sh.G, e.sh.R, e.sh.i16, e.gcups, k + 1 < table.size() ? "," : "");
+    std::fprintf(f,
+                 "  {\"out\": \"%s\", \"lo\": %d, \"hi\": %d, \"G\": %d, \"R\": %d, \"i16\": %d, \"cta\": %d, "
+                 "\"gcups\": %.1f}%s\n",
+                 kOutNames[e.out], e.lo, e.hi, e.sh.G, e.sh.R, e.sh.i16, e.cta, e.gcups, k + 1 < table.size() ? "," : "");
   }
   std::fprintf(f, " ]\n}\n");
   std::fclose(f);
