@@ -473,7 +473,67 @@ def serve_leg(n_requests=120, loads=(0.25, 0.5, 0.9), seed=5, plain_pairs=600):
     out["plain_gcups"] = sample_cells / t_plain / 1e9
     out["plain_pairs_sampled"] = done
     out["served_over_plain"] = out["capacity_gcups"] / out["plain_gcups"]
+
+    # The same workload with the device-resident request loop on (it takes
+    # the score requests whose pairs are all at most 2,048 residues long).
+    res = {}
+    with A.Server(slots=4, resident=True) as srv:
+        t0 = time.perf_counter()
+        ids = [srv.submit(r.pairs, **kw(r)) for r in reqs]
+        for rid in ids:
+            srv.poll(rid)
+        closed_s = time.perf_counter() - t0
+        st = srv.stats()
+    res["capacity_gcups"] = total / closed_s / 1e9
+    res["resident_requests"] = st["resident_requests"]
+    res["loads"] = []
+    rng = np.random.default_rng(seed + 1)
+    for load in loads:
+        lam = load * capacity / float(cells.mean())
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, size=len(reqs)))
+        st = _served_run(A, reqs, kw, arrivals, dict(slots=4, resident=True))
+        res["loads"].append({"offered": load, "achieved_gcups": total / st["span_s"] / 1e9, "p50_ms": st["p50_ms"],
+                             "p99_ms": st["p99_ms"], "max_ms": st["max_ms"]})
+    out["resident"] = res
+
+    # Editor-sized traffic: many small score and identity requests (1-64
+    # pairs, proteins or DNA of 50-1,000 residues) at 1,000 requests per
+    # second, through ticks and through the device-resident loop.
+    small = W.serving_stream(300, 1000.0, max_pairs=64, lo=50, hi=1000, seed=seed + 2)
+
+    def kw_small(r):
+        base = dict(matrix="dna", gap_open=5, gap_extend=2) if r.pairs.matrix == W.DNA else {}
+        return dict(base, output="identity" if r.traceback else "score")
+
+    arrivals = np.array([r.arrival_s for r in small])
+    small_cells = float(sum(r.pairs.cells for r in small))
+    sm = {"workload": f"{len(small)} requests, {sum(len(r.pairs) for r in small)} pairs, {small_cells:.3e} cells, "
+                      "1-64 pairs (log-uniform), protein or DNA, lengths 50-1000, score or identity, "
+                      "Poisson arrivals at 1,000 requests/s"}
+    for name, skw in (("ticks", dict(slots=4)), ("resident", dict(slots=4, resident=True))):
+        _served_run(A, small, kw_small, arrivals, skw)  # warm
+        st = _served_run(A, small, kw_small, arrivals, skw)
+        sm[name] = {"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+                    "achieved_gcups": small_cells / st["span_s"] / 1e9, "ticks": st["ticks"],
+                    "resident_requests": st["resident_requests"], "resident_launches": st["resident_launches"]}
+    out["small_requests"] = sm
     return out
+
+
+def _served_run(A, reqs, kw, arrivals, server_kw):
+    """Submits the requests at their arrival times (seconds from the start)
+    and polls them all; returns the server's statistics."""
+    with A.Server(**server_kw) as srv:
+        t0 = time.perf_counter()
+        ids = []
+        for r, t_arr in zip(reqs, arrivals):
+            delay = t0 + t_arr - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            ids.append(srv.submit(r.pairs, **kw(r)))
+        for rid in ids:
+            srv.poll(rid)
+        return srv.stats()
 
 
 def configs_leg(c3_pairs=12):

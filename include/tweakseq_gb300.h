@@ -184,7 +184,18 @@ void tsq_batch_destroy(tsq_batch *b);
  * results, band-boundary rows and, for alignments, traceback planes) fits
  * the HBM budget left by the ticks in flight, and runs up to `slots` ticks
  * at once on separate streams.  Each request's results equal those of
- * tsq_align_batch on that request alone. */
+ * tsq_align_batch on that request alone.
+ *
+ * With opts.resident, score and identity requests whose pairs are at most
+ * 2,048 residues long (and at most 65,536 pairs) go to a device-resident
+ * request loop instead: a persistent kernel on half the SMs, one pair per
+ * warp, takes the pairs of published requests from a task queue in device
+ * memory; the request's residues, codes, pair table and results live in a
+ * device arena until the request is polled, and completion is counted in
+ * mapped host memory.  The kernel's waits are bounded: after
+ * resident_idle_polls empty polls it ends, and the server relaunches it
+ * when work arrives.  The loop holds SM resources while it runs, so ticks
+ * running beside it get fewer blocks. */
 typedef struct tsq_server tsq_server;
 
 typedef struct {
@@ -193,6 +204,14 @@ typedef struct {
   int64_t hbm_budget_bytes; /* admission budget (0 = half the free HBM at creation) */
   int64_t max_tick_cells;   /* DP cells per tick before it closes (0 = 4e10) */
   int32_t autotune;         /* 1 = plan ticks with the tuned table */
+  int32_t resident;         /* 1 = device-resident request loop for score and
+                               identity requests of pairs up to 2,048 residues
+                               (a persistent kernel fed from a device task
+                               queue; see below) */
+  int32_t resident_idle_polls; /* empty-queue polls (about a microsecond apart
+                               at most) after which the loop's kernel ends;
+                               the server relaunches it when work arrives
+                               (0 = 1,048,576) */
   int32_t reserved;
 } tsq_server_opts;
 
@@ -204,6 +223,9 @@ typedef struct {
   int64_t admission_waits;      /* times the oldest request waited for memory */
   double p50_ms, p99_ms, max_ms; /* submit-to-completion latency */
   double span_s;                /* first submit to last completion */
+  int64_t resident_requests;    /* requests served by the device-resident loop */
+  int64_t resident_launches;    /* launches of the loop's kernel */
+  int64_t resident_idle_exits;  /* times its kernel ended after idle_polls empty polls */
 } tsq_server_stats;
 
 int tsq_server_create(const tsq_server_opts *opts, tsq_server **out);

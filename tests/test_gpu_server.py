@@ -151,3 +151,70 @@ def test_cancel_and_invalid_input():
             srv.submit(worse, output="score")
         assert e.value.rc == N.E_INVALID_ARG
         assert srv.cancel(123456789) == N.E_NOT_FOUND
+
+
+def _resident_requests(seed):
+    """Requests for the device-resident loop (score and identity, pairs up
+    to 2,048 residues, protein and DNA, global and local) mixed with ones it
+    does not take (alignments, a pair longer than 2,048) and one with an
+    invalid residue."""
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(16):
+        kind = k % 5
+        if kind == 0:
+            ps, kw = _protein_pairs(rng, int(rng.integers(1, 40)), 20, 700), dict(output="score")
+        elif kind == 1:
+            ps, kw = _protein_pairs(rng, int(rng.integers(20, 300)), 50, 1200), dict(output="identity", mode="local")
+        elif kind == 2:
+            ps = _dna_pairs(rng, int(rng.integers(1, 30)), 100, 2000)
+            kw = dict(matrix="dna", gap_open=5, gap_extend=2, output="score", mode="local")
+        elif kind == 3:
+            ps, kw = _protein_pairs(rng, int(rng.integers(1, 4)), 100, 400), dict(output="alignment")
+        else:
+            ps, kw = _protein_pairs(rng, int(rng.integers(5, 60)), 100, 1800), dict(output="identity")
+        reqs.append((ps, kw))
+    reqs.append((_protein_pairs(rng, 3, 2100, 2300), dict(output="score")))  # too long for the loop
+    bad = W._pairset_from_lists([b"ACDEFGHIK", b"ACDEFGHIK", b"AC*EF"], [(0, 1), (0, 2)])
+    reqs.append((bad, dict(output="score")))
+    return reqs
+
+
+def test_resident_loop_alone_and_in_the_mix():
+    """With the device-resident loop, every request's results equal
+    tsq_align_batch's on that request alone, submitted one at a time and
+    all at once; the loop takes exactly the eligible requests."""
+    reqs = _resident_requests(21)
+    alone = [A.align_batch(ps, check=False, **kw) for ps, kw in reqs]
+    eligible = sum(1 for ps, kw in reqs if kw["output"] != "alignment" and max(ps.a_len.max(), ps.b_len.max()) <= 2048)
+    with A.Server(slots=2, resident=True) as srv:
+        for (ps, kw), want in zip(reqs, alone):
+            rid = srv.submit(ps, **kw)
+            assert _same(srv.poll(rid, check=False), want)
+        ids = [srv.submit(ps, **kw) for ps, kw in reqs]
+        for k, rid in enumerate(ids):
+            assert _same(srv.poll(rid, check=False), alone[k]), k
+        st = srv.stats()
+        assert st["resident_requests"] == 2 * eligible
+        assert st["resident_launches"] >= 1
+        assert st["completed"] == 2 * len(reqs)
+    assert alone[-1].table["status"].tolist() == [0, N.E_INVALID_RESIDUE]
+
+
+def test_resident_loop_idle_exit_and_relaunch():
+    """The loop's kernel ends after its idle polls run out (a bounded wait,
+    reported in mapped memory) and is relaunched by the next request, whose
+    results are still exact."""
+    rng = np.random.default_rng(22)
+    ps = _protein_pairs(rng, 50, 50, 600)
+    want = A.align_batch(ps, output="score")
+    with A.Server(slots=1, resident=True, resident_idle_polls=200) as srv:
+        assert _same(srv.poll(srv.submit(ps, output="score")), want)
+        deadline = time.time() + 5.0
+        while srv.stats()["resident_idle_exits"] < 1 and time.time() < deadline:
+            time.sleep(0.01)
+        st = srv.stats()
+        assert st["resident_idle_exits"] >= 1
+        launches = st["resident_launches"]
+        assert _same(srv.poll(srv.submit(ps, output="score")), want)
+        assert srv.stats()["resident_launches"] == launches + 1

@@ -82,7 +82,8 @@ class BatchOpts(ctypes.Structure):
 
 class ServerOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("slots", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64),
-                ("max_tick_cells", ctypes.c_int64), ("autotune", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("max_tick_cells", ctypes.c_int64), ("autotune", ctypes.c_int32), ("resident", ctypes.c_int32),
+                ("resident_idle_polls", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class ServerStats(ctypes.Structure):
@@ -90,7 +91,8 @@ class ServerStats(ctypes.Structure):
                 ("cancelled", ctypes.c_int64), ("ticks", ctypes.c_int64), ("cells_completed", ctypes.c_int64),
                 ("peak_reserved_bytes", ctypes.c_int64), ("admission_waits", ctypes.c_int64),
                 ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
-                ("span_s", ctypes.c_double)]
+                ("span_s", ctypes.c_double), ("resident_requests", ctypes.c_int64),
+                ("resident_launches", ctypes.c_int64), ("resident_idle_exits", ctypes.c_int64)]
 
 
 class BatchStats(ctypes.Structure):

@@ -266,12 +266,18 @@ def probe_dpx(packed: bool = False) -> float:
 class Server:
     """Continuous-batching server (tsq_server_*): submit requests of any
     size from any thread, poll their results; the library's scheduler thread
-    groups, admits (by HBM budget) and overlaps them on the GPU."""
+    groups, admits (by HBM budget) and overlaps them on the GPU.  With
+    resident=True, score and identity requests of pairs up to 2,048 residues
+    go to the device-resident request loop (a persistent kernel fed from a
+    device task queue) instead of ticks."""
 
-    def __init__(self, slots=4, hbm_budget_bytes=0, max_tick_cells=0, autotune=False, device=-1):
+    def __init__(self, slots=4, hbm_budget_bytes=0, max_tick_cells=0, autotune=False, device=-1, resident=False,
+                 resident_idle_polls=0):
         o = N.ServerOpts()
         o.device, o.slots, o.hbm_budget_bytes, o.max_tick_cells = device, slots, hbm_budget_bytes, max_tick_cells
         o.autotune = int(bool(autotune))
+        o.resident = int(bool(resident))
+        o.resident_idle_polls = int(resident_idle_polls)
         h = ctypes.c_void_p()
         N.check(N.lib().tsq_server_create(ctypes.byref(o), ctypes.byref(h)), "tsq_server_create")
         self._h = h

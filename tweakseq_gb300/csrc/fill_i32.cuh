@@ -41,9 +41,14 @@ namespace tsq {
 namespace fill {
 
 // One warp task: the warp's 32/G groups each take one pair (or idle).
+// The group rings sit in the block's ring area at the warp's slots; with
+// warp_rings set they sit there instead, in a layout private to the warp
+// (the top rings of its groups, then their code rings), so that warps of
+// one block may run different output modes at once.
 template <int G, int R, bool LOCAL, int OUT>
 __device__ __forceinline__ void fill_warp_task(const FillArgs &A, const int8_t *s_mat, uint2 *s_prof,
-                                               uint8_t *s_rings, int begin, int count, int warp_id) {
+                                               uint8_t *s_rings, int begin, int count, int warp_id,
+                                               uint8_t *warp_rings = nullptr) {
   static_assert(R == 8, "the profile word layout assumes 8 rows per lane");
   using Top = typename TopT<OUT>::T;
   constexpr int GPW = 32 / G;  // groups per warp
@@ -61,8 +66,9 @@ __device__ __forceinline__ void fill_warp_task(const FillArgs &A, const int8_t *
   // This group's staging rings.
   const int gslot = (threadIdx.x >> 5) * 8 + gw;
   constexpr int kTopStride = kTopRing * int(sizeof(Top)) + kRingPad;  // bytes
-  Top *top_ring = reinterpret_cast<Top *>(s_rings + gslot * kTopStride);
-  uint8_t *code_ring = s_rings + kSlotsPerBlock * kTopStride + gslot * (kCodeRing + kRingPad);
+  Top *top_ring = reinterpret_cast<Top *>(warp_rings ? warp_rings + gw * kTopStride : s_rings + gslot * kTopStride);
+  uint8_t *code_ring = warp_rings ? warp_rings + GPW * kTopStride + gw * (kCodeRing + kRingPad)
+                                  : s_rings + kSlotsPerBlock * kTopStride + gslot * (kCodeRing + kRingPad);
 
   {
     const bool have = gw < count;

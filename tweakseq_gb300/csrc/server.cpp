@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "resident.h"
 #include "trace.h"
 
 namespace {
@@ -52,6 +53,12 @@ struct Request {
   enum State { kPending, kRunning, kDone, kCancelled } state = kPending;
   int32_t status = TSQ_OK;
   std::vector<tsq_result> results;
+  // Served by the device-resident loop: its slot and arena range, and
+  // whether its results are still in the arena.
+  bool resident = false;
+  int32_t rslot = -1;
+  tsq::resident::Range rrange;
+  bool on_device = false;
 };
 
 struct Slot {
@@ -105,6 +112,13 @@ struct tsq_server {
   std::vector<double> latencies_ms;
   Clock::time_point t_first_submit, t_last_done;
   bool any_submit = false;
+  // The device-resident request loop (opts.resident).
+  std::unique_ptr<tsq::resident::Loop> loop;
+  std::deque<std::shared_ptr<Request>> rpending;     // waiting for arena room
+  std::vector<std::shared_ptr<Request>> rrunning;    // published, not done
+  int64_t resident_requests = 0;
+  int64_t r_outstanding_pairs = 0;
+  int tend_resident();                               // called with the lock held
 
   // Boundary rows a tick of npairs pairs needs for sequences up to max_n
   // columns: 8 group rows per warp of the launch (no more warps than pairs,
@@ -184,10 +198,75 @@ void tsq_server::finish(Slot &s, int rc) {
   cv_done.notify_all();
 }
 
+// The resident loop's side of the scheduler (lock held): finished
+// requests, admission and publication of waiting ones, and a relaunch of
+// the loop's kernel when it has ended with work outstanding.  Returns
+// whether resident requests are in flight.
+int tsq_server::tend_resident() {
+  if (!loop) return 0;
+  const auto now = Clock::now();
+  for (size_t k = 0; k < rrunning.size();) {
+    Request &r = *rrunning[k];
+    const int64_t n = int64_t(r.pairs.size());
+    if (!loop->done(r.rslot, n)) {
+      ++k;
+      continue;
+    }
+    loop->retired(n);
+    r_outstanding_pairs -= n;
+    r.state = Request::kDone;
+    r.on_device = true;
+    r.t_done = now;
+    ++completed;
+    cells_done += r.cells;
+    latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r.t_submit).count());
+    t_last_done = now;
+    rrunning.erase(rrunning.begin() + int64_t(k));
+    cv_done.notify_all();
+  }
+  while (!rpending.empty() && !stop) {
+    const std::shared_ptr<Request> r = rpending.front();
+    const int64_t n = int64_t(r->pairs.size());
+    if (r_outstanding_pairs + n > tsq::resident::kRingCap) break;
+    int32_t slot = -1;
+    tsq::resident::Range range;
+    const int rc = loop->admit(int64_t(r->seqs.size()), n, &slot, &range);
+    if (rc == TSQ_E_PENDING) {
+      ++admission_waits;
+      break;
+    }
+    rpending.pop_front();
+    if (rc) {
+      r->status = rc;
+      r->state = Request::kDone;
+      ++completed;
+      cv_done.notify_all();
+      continue;
+    }
+    r->rslot = slot;
+    r->rrange = range;
+    r->state = Request::kRunning;
+    const int prc = loop->publish(slot, range, r->seqs, r->pairs, r->params, r->custom_score, r->custom_valid);
+    if (prc) {
+      loop->release(slot, range);
+      r->status = prc;
+      r->state = Request::kDone;
+      ++completed;
+      cv_done.notify_all();
+      continue;
+    }
+    r_outstanding_pairs += n;
+    rrunning.push_back(r);
+  }
+  loop->tend();
+  return rrunning.empty() ? 0 : 1;
+}
+
 void tsq_server::run() {
   cudaSetDevice(device);
   std::unique_lock<std::mutex> lock(mu);
   for (;;) {
+    const int resident_busy = tend_resident();
     // Completed ticks.
     for (Slot &s : slots)
       if (s.busy) {
@@ -195,7 +274,7 @@ void tsq_server::run() {
         if (q != TSQ_E_PENDING) finish(s, q);
       }
     if (stop) {
-      bool busy = false;
+      bool busy = resident_busy != 0;
       for (Slot &s : slots) busy |= s.busy;
       if (!busy) break;
     }
@@ -256,10 +335,12 @@ void tsq_server::run() {
       }
     }
     if (!launched) {
-      bool busy = false;
+      bool busy = resident_busy != 0 || !rpending.empty();
       for (Slot &s : slots) busy |= s.busy;
-      // Poll in-flight ticks often; sleep longer when idle.
-      cv_work.wait_for(lock, busy ? std::chrono::microseconds(50) : std::chrono::milliseconds(2));
+      // Poll in-flight work often (resident requests most often: their
+      // completion is one read of mapped memory); sleep longer when idle.
+      cv_work.wait_for(lock, resident_busy ? std::chrono::microseconds(10)
+                                           : (busy ? std::chrono::microseconds(50) : std::chrono::milliseconds(2)));
     }
   }
 }
@@ -287,6 +368,15 @@ int tsq_server_create(const tsq_server_opts *opts, tsq_server **out) {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return TSQ_E_CUDA;
     s->resident_warps = sms * 16;  // most warps any fill kernel keeps resident per SM
+    if (s->opts.resident) {
+      // The loop's arena comes out of the budget: a quarter of it, at most
+      // 4 GiB.
+      const int64_t arena = std::min<int64_t>(s->opts.hbm_budget_bytes / 4, int64_t(4) << 30);
+      s->loop.reset(new tsq::resident::Loop());
+      const int rc = s->loop->init(dev, arena, s->opts.resident_idle_polls);
+      if (rc) return rc;
+      s->opts.hbm_budget_bytes -= arena;
+    }
     s->slots.resize(size_t(s->opts.slots));
     tsq_server *raw = s.get();
     s->worker = std::thread([raw]() { raw->run(); });
@@ -328,9 +418,10 @@ int tsq_server_submit(tsq_server *s, const uint8_t *seqs, int64_t seqs_len, cons
         bytes += tsq::plane_bytes(d.a_len, d.b_len, tsq::Shape{32, 8, 0}) + 2 * (int64_t(d.a_len) + d.b_len);
     }
     r->bytes = bytes;
+    r->resident = s->loop && tsq::resident::Loop::eligible(r->params, r->pairs);
     std::lock_guard<std::mutex> lock(s->mu);
     if (s->stop) return TSQ_E_CANCELLED;
-    if (r->bytes + s->boundary_bytes(r->max_n, n) > s->opts.hbm_budget_bytes) {
+    if (!r->resident && r->bytes + s->boundary_bytes(r->max_n, n) > s->opts.hbm_budget_bytes) {
       ++s->rejected;
       return TSQ_E_REJECTED;
     }
@@ -342,7 +433,12 @@ int tsq_server_submit(tsq_server *s, const uint8_t *seqs, int64_t seqs_len, cons
     }
     ++s->submitted;
     s->requests[r->id] = r;
-    s->pending.push_back(r);
+    if (r->resident) {
+      ++s->resident_requests;
+      s->rpending.push_back(r);
+    } else {
+      s->pending.push_back(r);
+    }
     *request_id = r->id;
     s->cv_work.notify_one();
     return TSQ_OK;
@@ -369,6 +465,19 @@ int tsq_server_poll(tsq_server *s, uint64_t id, int32_t wait_ms, tsq_result *out
     return TSQ_E_CANCELLED;
   }
   if (r->state != Request::kDone) return TSQ_E_PENDING;
+  if (r->on_device) {
+    // A resident request's results leave the device arena when polled.
+    const int64_t np = int64_t(r->pairs.size());
+    if (n != np || (n > 0 && !out)) return TSQ_E_INVALID_ARG;
+    r->on_device = false;
+    lock.unlock();
+    const int st = s->loop->fetch(r->rrange, int64_t(r->seqs.size()), np, out);
+    lock.lock();
+    s->loop->release(r->rslot, r->rrange);
+    s->requests.erase(id);
+    s->cv_work.notify_one();  // arena room for waiting requests
+    return st;
+  }
   if (n != int64_t(r->results.size()) || (n > 0 && !out)) return TSQ_E_INVALID_ARG;
   // The strings move to the caller, who frees them with tsq_results_free.
   std::copy(r->results.begin(), r->results.end(), out);
@@ -384,11 +493,12 @@ int tsq_server_cancel(tsq_server *s, uint64_t id) {
   if (it == s->requests.end()) return TSQ_E_NOT_FOUND;
   Request &r = *it->second;
   if (r.state != Request::kPending) return TSQ_E_PENDING;  // already on the device (or done)
-  for (auto p = s->pending.begin(); p != s->pending.end(); ++p)
-    if ((*p)->id == id) {
-      s->pending.erase(p);
-      break;
-    }
+  for (auto *q : {&s->pending, &s->rpending})
+    for (auto p = q->begin(); p != q->end(); ++p)
+      if ((*p)->id == id) {
+        q->erase(p);
+        break;
+      }
   r.state = Request::kCancelled;
   ++s->cancelled;
   s->cv_done.notify_all();
@@ -412,6 +522,11 @@ int tsq_server_get_stats(tsq_server *s, tsq_server_stats *st) {
   st->max_ms = s->latencies_ms.empty() ? 0.0 : *std::max_element(s->latencies_ms.begin(), s->latencies_ms.end());
   if (s->any_submit && s->completed > 0)
     st->span_s = std::chrono::duration<double>(s->t_last_done - s->t_first_submit).count();
+  st->resident_requests = s->resident_requests;
+  if (s->loop) {
+    st->resident_launches = s->loop->launches();
+    st->resident_idle_exits = s->loop->idle_exits();
+  }
   return TSQ_OK;
 }
 
@@ -420,17 +535,20 @@ int tsq_server_destroy(tsq_server *s) {
   {
     std::lock_guard<std::mutex> lock(s->mu);
     s->stop = true;
-    for (auto &r : s->pending) {
-      r->state = Request::kCancelled;
-      ++s->cancelled;
+    for (auto *q : {&s->pending, &s->rpending}) {
+      for (auto &r : *q) {
+        r->state = Request::kCancelled;
+        ++s->cancelled;
+      }
+      q->clear();
     }
-    s->pending.clear();
     s->cv_work.notify_all();
     s->cv_done.notify_all();
   }
   if (s->worker.joinable()) s->worker.join();
   for (auto &kv : s->requests) tsq_results_free(kv.second->results.data(), int64_t(kv.second->results.size()));
   cudaSetDevice(s->device);
+  s->loop.reset();  // stops the loop's kernel, frees its arena
   delete s;
   return TSQ_OK;
 }
