@@ -62,7 +62,11 @@ extern "C" {
 
 /* What to compute. */
 #define TSQ_OUT_SCORE 0     /* score (local: plus end coordinates) */
-#define TSQ_OUT_IDENTITY 1  /* score, n_ident and n_cols, no strings */
+#define TSQ_OUT_IDENTITY 1  /* score, n_ident and n_cols, no strings; a pair
+                               with a_len + b_len > 65,535 gets
+                               TSQ_E_TOO_LARGE (the two counts travel
+                               together in 32 bits) -- use
+                               TSQ_OUT_ALIGNMENT for longer pairs */
 #define TSQ_OUT_ALIGNMENT 2 /* everything, gapped strings included */
 
 /* DP lane width. */
@@ -95,7 +99,11 @@ typedef struct {
   char *aln_b;
 } tsq_result;
 
-/* One pair of a batch: offsets and lengths into the batch's residue buffer. */
+/* One pair of a batch: offsets and lengths into the batch's residue buffer.
+ * Per-pair limits (beyond them the pair gets TSQ_E_TOO_LARGE): each
+ * sequence at most 1,048,575 residues; 3*gap_open + (a_len + b_len + 1) *
+ * gap_extend below 2^28 (the int32 fill's range); identity output a_len +
+ * b_len <= 65,535; local mode max_score * min(a_len, b_len) below 2^23. */
 typedef struct {
   int64_t a_off, b_off;
   int32_t a_len, b_len;
