@@ -294,6 +294,91 @@ def test_int16_overflow_rerun_and_lane_choices(local):
         assert b.stats()["rerun_pairs"] >= 3  # 2979, 3100 and 3500 overflow (2978 is flagged too)
 
 
+def _overflow_edge_pairs(seed, n_random, hi):
+    """W:W homopolymers around the int16 edge (W scores 11 per residue, so
+    2978 residues is the longest proven pair) plus ordinary random pairs."""
+    rng = np.random.default_rng(seed)
+    seqs, pairs = [], []
+    for L in (2900, 2978, 2979, 3100):
+        seqs += [b"W" * L, b"W" * L]
+        pairs.append((len(seqs) - 2, len(seqs) - 1))
+    for k in range(n_random):
+        a = W.random_protein(rng, int(rng.integers(1, hi))).tobytes()
+        b = W.random_protein(rng, int(rng.integers(1, hi))).tobytes()
+        seqs += [a, b]
+        pairs.append((len(seqs) - 2, len(seqs) - 1))
+    return W._pairset_from_lists(seqs, pairs)
+
+
+@pytest.mark.parametrize("output,local", [("alignment", False), ("alignment", True), ("identity", False)])
+def test_int16_traceback_and_identity_fills_at_the_overflow_edge(output, local):
+    """The int16x2 traceback and identity fills: pairs past the proven int16
+    range are flagged by the checked kernel and re-run in int32 (planes and
+    counts rewritten), pairs at the edge stay in int16x2; every lane choice
+    gives the oracle's scores, counts and strings."""
+    ps = _overflow_edge_pairs(37, 40, 900)
+    mode = "local" if local else "global"
+    if output == "alignment":
+        want, sa, sb = oracle_batch(ps, local, O.MODE_ALIGN, strings=True)
+        fields = FIELDS
+    else:
+        want, sa, sb = oracle_batch(ps, local, O.MODE_IDENT), None, None
+        fields = ident_fields(local)
+    for lane in ("auto", "i16", "i32"):
+        got = A.align_batch(ps, mode=mode, output=output, lane=lane)
+        assert_same(got, want, fields, f"{output} lane {lane}")
+        if sa is not None:
+            assert got.aln_a == sa and got.aln_b == sb, f"strings, lane {lane}"
+    with A.Batch(ps, mode=mode, output=output, lane="auto") as b:
+        b.run()
+        assert_same(b.results(), want, fields, "batch")
+        assert b.stats()["rerun_pairs"] >= 2  # 2979 and 3100 overflow
+
+
+@pytest.mark.parametrize("dna", [False, True])
+def test_int16_and_int32_lanes_agree_all_outputs(dna):
+    """Uneven pairs (proteins, or DNA at +2/-3) through the int16x2 fills
+    (lane auto) and the int32 fills (lane i32): both equal the oracle for
+    every output, global and local, including open 0 and extend 0 gaps."""
+    ps = random_pairs(53 + dna, 300, 0, 1200 if dna else 700, dna=dna)
+    gap_sets = ((ps.gap_open, ps.gap_extend), (0, 2), (4, 0))
+    for go, ge in gap_sets:
+        q = dataclasses.replace(ps, gap_open=go, gap_extend=ge)
+        for local in (False, True):
+            want, sa, sb = oracle_batch(q, local, O.MODE_ALIGN, strings=True)
+            wid = oracle_batch(q, local, O.MODE_IDENT)
+            for lane in ("auto", "i32"):
+                got = gpu_batch(q, local, "alignment", lane=lane)
+                assert_same(got, want, FIELDS, f"alignment gaps {go}/{ge} local {local} lane {lane}")
+                assert got.aln_a == sa and got.aln_b == sb, f"strings gaps {go}/{ge} local {local} lane {lane}"
+                gi = gpu_batch(q, local, "identity", lane=lane)
+                assert_same(gi, wid, ident_fields(local), f"identity gaps {go}/{ge} local {local} lane {lane}")
+
+
+def test_identity_counts_letters_sharing_a_score_class():
+    """J, O, U and X score alike under BLOSUM62 (one score class) but are
+    different letters: the identity fill counts only equal letters."""
+    rng = np.random.default_rng(77)
+    alpha = np.frombuffer(b"JOUXBZ" + b"ARNDCQEGHILKMFPSTWYV", dtype=np.uint8)
+    seqs, pairs = [], []
+    for k in range(200):
+        a = alpha[rng.integers(0, 8 if k % 2 else len(alpha), int(rng.integers(1, 400)))]
+        b = a.copy()
+        flip = rng.random(len(b)) < 0.3
+        b[flip] = alpha[rng.integers(0, 6, int(flip.sum()))]
+        seqs += [a.tobytes(), b.tobytes()]
+        pairs.append((2 * k, 2 * k + 1))
+    ps = W._pairset_from_lists(seqs, pairs)
+    want = oracle_batch(ps, False, O.MODE_IDENT)
+    for lane in ("auto", "i16", "i32"):
+        got = gpu_batch(ps, False, "identity", lane=lane)
+        assert_same(got, want, ident_fields(False), f"identity lane {lane}")
+    want_a, sa, sb = oracle_batch(ps, False, O.MODE_ALIGN, strings=True)
+    got = gpu_batch(ps, False, "alignment")
+    assert_same(got, want_a, FIELDS, "alignment")
+    assert got.aln_a == sa and got.aln_b == sb
+
+
 def test_mixed_lane_types_one_batch():
     """One batch whose pairs split over int16x2, checked int16x2 and int32:
     with extend 60 the lower bound only fits int16 for short pairs."""

@@ -25,6 +25,7 @@ def _write(tmp_path, entries):
 def test_table_with_lane_type_and_cta_loads(lib, tmp_path):
     entries = [{"out": "score", "lo": 0, "hi": 512, "G": 4, "R": 8, "i16": 1, "cta": 0, "gcups": 1.0},
                {"out": "score", "lo": 512, "hi": 4096, "G": 8, "R": 8, "i16": 0, "cta": 1, "gcups": 1.0},
+               {"out": "identity", "lo": 0, "hi": 512, "G": 8, "R": 8, "i16": 1, "cta": 0, "gcups": 1.0},
                {"out": "alignment", "lo": 0, "hi": 1 << 21, "G": 32, "R": 8, "i16": 0, "cta": 1, "gcups": 1.0}]
     assert lib.tsq_tune_load(_write(tmp_path, entries)) == N.TSQ_OK
     # A table written before the CTA choice (no "cta" key) still loads.
@@ -35,7 +36,8 @@ def test_table_with_lane_type_and_cta_loads(lib, tmp_path):
 
 @pytest.mark.parametrize("bad", [
     {"cta": 2},                      # not a flag
-    {"i16": 1, "out": "identity"},   # int16x2 lanes fill score output only
+    {"i16": 2},                      # not a flag
+    {"R": 16},                       # rows per lane are fixed at 8
     {"G": 6},                        # no such lane width
     {"lo": 100, "hi": 100},          # empty bucket
     {"out": "trace"},                # unknown output kind

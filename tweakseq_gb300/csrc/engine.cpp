@@ -340,6 +340,11 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
               const tsq_pair_desc *pairs, int64_t n, const tsq_params *p, const tsq_batch_opts *opts, bool plain,
               int64_t call_pairs, int64_t call_cells, bool segmented);
 int prepare_object(tsq_batch *b, const tsq_params *p, const tsq_batch_opts *opts, Scheme *sc, int *sms);
+// int16x2 fills exist for every output but local identity.
+bool lanes16_possible(int out_mode, bool local, int lane) {
+  return lane != TSQ_LANE_I32 && !(out_mode == kOutIdent && local);
+}
+
 int out_mode_of(const tsq_params *p) {
   return p->output == TSQ_OUT_ALIGNMENT ? kOutTrace : (p->output == TSQ_OUT_IDENTITY ? kOutIdent : kOutScore);
 }
@@ -389,7 +394,7 @@ int input_prepare(tsq_batch *owner, int64_t seqs_len, const tsq_params *p, const
   int rc = prepare_object(owner, p, opts, &sc, &sms);
   if (rc) return rc;
   cudaStream_t st = owner->stream;
-  owner->classes = out_mode_of(p) == kOutScore && p->lane != TSQ_LANE_I32;
+  owner->classes = lanes16_possible(out_mode_of(p), p->mode == TSQ_LOCAL, p->lane);
   owner->seqs_len = seqs_len;
   TSQ_TRY(owner->seqs.ensure(size_t(seqs_len) + 128, st, owner->async_max));
   TSQ_TRY(owner->codes.ensure(size_t(seqs_len) + 128, st, owner->async_max));
@@ -552,8 +557,8 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
     cudaStream_t st;
     ~SyncOnExit() { cudaStreamSynchronize(st); }
   } sync_on_exit{b->stream};
-  // Score batches also get class codes for the int16x2 fill.
-  b->classes = b->out_mode == kOutScore && p->lane != TSQ_LANE_I32;
+  // Batches that may run int16x2 fills also get class codes.
+  b->classes = lanes16_possible(b->out_mode, b->local, p->lane);
   if (!b->input_owner) {
     TSQ_TRY(b->seqs.ensure(size_t(seqs_len) + 128, b->stream, b->async_max));
     TSQ_TRY(b->codes.ensure(size_t(seqs_len) + 128, b->stream, b->async_max));
@@ -630,7 +635,7 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
     const double lanes = double(sms) * 24.0 * 32.0;
     const double cta_budget = std::max(20000.0, plain ? 0.0 : double(shape_cells) / (lanes * kR));
     const int64_t go = p->gap_open, ge = p->gap_extend;
-    const bool try16 = b->out_mode == kOutScore && p->lane != TSQ_LANE_I32;
+    const bool try16 = lanes16_possible(b->out_mode, b->local, p->lane);
     const int64_t smax = std::max(sc.max_score, 0), sneg = std::max<int64_t>(0, -int64_t(sc.min_score));
     parallel_for(n, [&](int64_t lo, int64_t hi, int slot) {
       ShapePart sp;

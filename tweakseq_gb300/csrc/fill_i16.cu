@@ -1,5 +1,6 @@
-// fill_i16.cu -- the int16x2 score fills (plain and overflow-checked) and
-// the overflow collector of the int32 re-run.
+// fill_i16.cu -- the int16x2 score fills (plain and overflow-checked), the
+// shared-memory size of every int16x2 fill and the overflow collector of
+// the int32 re-run.
 #include <algorithm>
 
 #include "fill_i16.cuh"
@@ -7,41 +8,12 @@
 namespace tsq {
 namespace fill {
 
-cudaError_t launch_i16(bool check, bool local, const FillArgs &args, int blocks, size_t smem, cudaStream_t st) {
-  FillArgs a = args;
-  a.one = 1u;
-  if (check) {
-    if (local)
-      fill_i16_kernel<true, true><<<blocks, kThreads16, smem, st>>>(a);
-    else
-      fill_i16_kernel<false, true><<<blocks, kThreads16, smem, st>>>(a);
-  } else {
-    if (local)
-      fill_i16_kernel<true, false><<<blocks, kThreads16, smem, st>>>(a);
-    else
-      fill_i16_kernel<false, false><<<blocks, kThreads16, smem, st>>>(a);
-  }
-  return cudaGetLastError();
-}
+template cudaError_t launch_i16<kOutScore>(bool, bool, const FillArgs &, int, size_t, cudaStream_t);
+template int occupancy_i16<kOutScore>(bool, bool, size_t);
 
-size_t smem_i16(int nclasses);
-
-int occupancy_i16(bool check, bool local, size_t smem) {
-  auto k = check ? (local ? fill_i16_kernel<true, true> : fill_i16_kernel<false, true>)
-                 : (local ? fill_i16_kernel<true, false> : fill_i16_kernel<false, false>);
-  // The attribute allows the largest profile (26 classes), so that every
-  // scheme's launch fits whatever scheme was sized first.
-  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(std::max(smem, smem_i16(kLetters)))) !=
-      cudaSuccess)
-    return 0;
-  int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kThreads16, smem) != cudaSuccess) return 0;
-  return nb;
-}
-
-size_t smem_i16(int nclasses) {
-  return size_t(kMatBytes16) + size_t(2 * nclasses) * kThreads16 * sizeof(uint2) +
-         size_t(kSlots16) * (kTopRing * sizeof(uint32_t) + kCodeRing16 + 2 * kRingPad);
+size_t smem_i16(int out_mode, int nclasses) {
+  return size_t(kMatBytes16) + smem16_prof_bytes(nclasses) + smem16_match_bytes(out_mode, nclasses) +
+         size_t(kSlots16) * (smem16_top_stride(out_mode) + kCodeRing16 + kRingPad);
 }
 
 namespace {

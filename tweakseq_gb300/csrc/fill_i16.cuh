@@ -1,5 +1,6 @@
-// fill_i16.cuh -- group-striped Gotoh fill, score only, in packed int16x2
-// with DPX instructions (two cells per instruction).
+// fill_i16.cuh -- group-striped Gotoh fill in packed int16x2 with DPX
+// instructions (two cells per instruction): score, traceback planes, or
+// identity counts (global).
 //
 // Same recurrences and work split as the int32 fill (fill_i32.cuh), with two
 // row bands per pass packed into the two 16-bit halves of every register:
@@ -37,8 +38,35 @@
 // running maximum of H and flags the pair for an exact int32 re-run when it
 // comes within max_score of 32767 (an overflow must pass through such a
 // value first, since one diagonal step adds at most max_score).
+//
+// Decisions (traceback and identity fills).  Every decision of the
+// recurrences is a zero test of a difference between a maximum and one of
+// its operands: E opened iff e - T = 0, F opened iff f - XO = 0, H from the
+// diagonal iff h - dd = 0, from E iff h - x = 0 < x - dd.  A DPX maximum is
+// taken per half, so each such difference is >= 0 in both halves whatever
+// the values (even in halves outside their column range), and one 32-bit
+// subtraction computes both without a borrow crossing the halves;
+// min(difference, 1) per half is then the decision bit of each cell.  With
+// open >= 0 the F decision taken from X instead of H differs from the
+// int32 fill's only when open = 0 and F beats X strictly; both then walk
+// through the same cells and count the same columns.
+//
+// Traceback: per row, the nibble dir | E-open << 2 | F-open << 3 (dir =
+// [h > dd] + [h > x], or 3 for a local stop) is summed into two words by
+// integer multiply-adds (rows 0-3 and 4-7, band A in the low halves, band
+// B in the high halves), and two PRMTs give each band's 32-bit plane word.
+// The planes have the int32 fill's layout -- band A of pass p is band 2p,
+// band B band 2p+1, step index column + lane -- so the walker reads either.
+//
+// Identity (global): each cell carries two packed counts along its
+// optimal path, identical columns I and diagonal columns D (columns =
+// m + n - D); E, F and H pick theirs with the decision masks (0xFFFF per
+// half) by LOP3 selects, and the diagonal adds the match bit and 1.  The
+// profile is indexed by letter (every letter its own class), and a second
+// per-thread table holds, for each letter, the rows of the lane it matches.
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 
 #include "fill_common.cuh"
@@ -47,8 +75,11 @@ namespace tsq {
 namespace fill {
 
 // 4 warps per block; shared memory (each thread's profile rows, each
-// group's rings) allows 3 blocks per SM.  (2-warp blocks, 14 warps per SM
-// instead of 12, measured no faster: the ALU pipe is the limit.)
+// group's rings) allows 3 blocks per SM, 2 for the identity fill (26-letter
+// profile, match table, 16-byte ring entries).  (2-warp blocks, 14 warps per
+// SM instead of 12, measured no faster: the ALU pipe is the limit.)  No
+// minimum-blocks bound: with one, ptxas gives the score fill 128 registers
+// instead of 96.
 constexpr int kThreads16 = 128;
 constexpr int kSlots16 = kThreads16 / 32 * 8;
 constexpr int kCodeRing16 = 256;  // band B reads codes up to 2G columns behind band A
@@ -61,6 +92,18 @@ constexpr uint32_t kNeg2 = 0x03000300u;   // kNeg16 in both (biased) halves
 // profile is built from whole rows (four classes per word).
 constexpr int kMatRow16 = 32;
 constexpr int kMatBytes16 = (kLetters + 1) * kMatRow16 + 32;  // 896, a 64-byte multiple
+
+// Top-row entry carried from pass to pass: (H, F) of band B's bottom row as
+// biased halves; identity fills add the path counts (I, D) of that H and of
+// that F.
+template <int OUT>
+struct Top16 {
+  using T = uint32_t;
+};
+template <>
+struct Top16<kOutIdent> {
+  using T = uint4;
+};
 
 __device__ __forceinline__ uint32_t pack2(int32_t lo, int32_t hi) {
   return (uint32_t(lo) & 0xFFFFu) | (uint32_t(hi) << 16);
@@ -77,6 +120,21 @@ __device__ __forceinline__ uint32_t sub2_imad(uint32_t a, uint32_t one, uint32_t
   uint32_t d;
   asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(one), "r"(neg_sub2));
   return d;
+}
+
+// a * b + c on the FMA pipe (b an opaque run-time value, so that the
+// multiply-add is not turned into shifts and adds on the ALU pipe).
+__device__ __forceinline__ uint32_t imad(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+
+// Decision bits: 1 in each half where the difference hi - lo (>= 0 in
+// both halves, so the subtraction never borrows across them) is not zero.
+// minus_one is the opaque -1; k1 is 0x00010001.
+__device__ __forceinline__ uint32_t nz2(uint32_t hi, uint32_t lo, uint32_t minus_one, uint32_t k1) {
+  return __vimin3_u16x2(imad(lo, minus_one, hi), k1, k1);
 }
 
 // (sign-extended byte K of a, sign-extended byte K of b) as int16x2.
@@ -101,6 +159,10 @@ __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
   asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(sel));
   return d;
 }
+
+// The (H, F) word of a top-row entry.
+__device__ __forceinline__ uint32_t top_hf(uint32_t v) { return v; }
+__device__ __forceinline__ uint32_t top_hf(const uint4 &v) { return v.x; }
 
 
 // 4x4 byte transpose: w[i] holds bytes (x_i0, x_i1, x_i2, x_i3); o[k]
@@ -145,10 +207,12 @@ __device__ __forceinline__ bool range_has_bad(const uint8_t *p, int len, int t, 
 
 // The lane width G is a run-time value: one code path serves every width,
 // which keeps the kernel small enough for the instruction cache.
-template <bool LOCAL, bool CHECK>
+template <bool LOCAL, bool CHECK, int OUT>
 __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t *s_mat, uint2 *s_prof,
-                                                 uint8_t *s_rings, int begin, int count, int warp_id, int G,
-                                                 int lg) {
+                                                 uint32_t *s_match, uint8_t *s_rings, int begin, int count,
+                                                 int warp_id, int G, int lg) {
+  static_assert(!(OUT == kOutIdent && LOCAL), "the int16x2 identity fill is global only");
+  using Top = typename Top16<OUT>::T;
   constexpr int R = 8;
   const int P = G * R;   // rows per band
   const int P2 = 2 * P;  // rows per pass (bands A and B)
@@ -160,10 +224,17 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
   const uint32_t one = A.one;
   const uint32_t neg_oe2 = 0u - ((uint32_t(oe) << 16) | uint32_t(oe));  // adds -(oe, oe) without borrows
   const uint32_t zero_oe2 = pack2b(-oe, -oe);                          // max(x, 0) - oe floor, local
-  uint32_t *top = reinterpret_cast<uint32_t *>(A.bnd) + ((int64_t)warp_id * 8 + gw) * A.bnd_cols;
+  // Opaque constants of the decision arithmetic (multipliers of the FMA
+  // pipe's multiply-adds).
+  const uint32_t minus_one = 0u - one, k1 = one * 0x00010001u;
+  const uint32_t m4 = 0u - 4u * one, m8 = 0u - 8u * one;  // traceback: -4, -8
+  const uint32_t k16 = one << 4, k256 = one << 8, k4096 = one << 12;
+  const uint32_t kffff = one * 0xFFFFu;  // identity: decision bits to half masks
+  (void)minus_one, (void)k1, (void)m4, (void)m8, (void)k16, (void)k256, (void)k4096, (void)kffff, (void)s_match;
+  Top *top = reinterpret_cast<Top *>(A.bnd) + ((int64_t)warp_id * 8 + gw) * A.bnd_cols;
   const int gslot = (threadIdx.x >> 5) * 8 + gw;
-  constexpr int kTopStride = kTopRing * 4 + kRingPad;  // bytes
-  uint32_t *top_ring = reinterpret_cast<uint32_t *>(s_rings + gslot * kTopStride);
+  constexpr int kTopStride = kTopRing * int(sizeof(Top)) + kRingPad;  // bytes
+  Top *top_ring = reinterpret_cast<Top *>(s_rings + gslot * kTopStride);
   uint8_t *code_ring = s_rings + kSlots16 * kTopStride + gslot * (kCodeRing16 + kRingPad);
   const uint2 *profA = s_prof + threadIdx.x;                // + (2c) * kThreads16
   const uint2 *profB = s_prof + kThreads16 + threadIdx.x;   // + (2c) * kThreads16
@@ -204,13 +275,29 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
     max_steps = max(max_steps, __shfl_xor_sync(0xffffffffu, max_steps, o));
   }
 
-  // Row 0 of the matrix becomes the first top row: (H, F) as int16 halves.
-  if (!trivial)
-    for (int j = t; j < n; j += G) top[j] = pack2b(edge_h(j + 1, go, ge, LOCAL), kNeg16);
+  // Row 0 of the matrix becomes the first top row: (H, F) as int16 halves
+  // (path counts 0).
+  if (!trivial) {
+    for (int j = t; j < n; j += G) {
+      const uint32_t hf = pack2b(edge_h(j + 1, go, ge, LOCAL), kNeg16);
+      if constexpr (OUT == kOutIdent)
+        top[j] = make_uint4(hf, 0u, 0u, 0u);
+      else
+        top[j] = hf;
+    }
+  }
   __syncwarp();
+  // Traceback planes of the pair: band b, step s (column + lane), lane t
+  // at word (b * (n + G - 1) + s) * G + t; bands past the last real row
+  // have no words.
+  uint32_t *planes = nullptr;
+  const int nbands = (m + P - 1) / P;
+  if constexpr (OUT == kOutTrace) planes = reinterpret_cast<uint32_t *>(A.planes + (have ? A.plane_off[pid] : 0));
+  (void)planes, (void)nbands;
 
   int32_t lbest = 0, lrow = 0, lcol = 0;
   int32_t last_h = 0;
+  uint32_t last_i = 0, last_d = 0;  // identity: counts of H(m, n)
   uint32_t hmax = LOCAL ? kBias2 : kNeg2;
 
   for (int pass = 0; pass < max_passes; ++pass) {
@@ -250,10 +337,25 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
           }
         }
       }
+      if constexpr (OUT == kOutIdent) {
+        // Match table: for each letter, bit r (band A) and bit 16 + r
+        // (band B) set where row r of the lane holds that letter.  Padding
+        // rows (class ncls) match nothing.
+        for (int c = 0; c < ncls; ++c) s_match[c * kThreads16 + threadIdx.x] = 0u;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int ca = xa[r] / kMatRow16, cb2 = xb[r] / kMatRow16;
+          if (ca < ncls) s_match[ca * kThreads16 + threadIdx.x] |= 1u << r;
+          if (cb2 < ncls) s_match[cb2 * kThreads16 + threadIdx.x] |= 1u << (16 + r);
+        }
+      }
     }
 
     uint32_t H[R], E[R], T[R];
     uint32_t best[R], bcol[R];
+    // Identity: counts (I, D) of H and E per row.
+    uint32_t IH[R], DH[R], IE[R], DE[R];
+    (void)IH, (void)DH, (void)IE, (void)DE;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       H[r] = pack2b(edge_h(rowA + r + 1, go, ge, LOCAL), edge_h(rowB + r + 1, go, ge, LOCAL));
@@ -261,26 +363,43 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       E[r] = kNeg2;
       best[r] = kBias2;
       bcol[r] = 0u;
+      if constexpr (OUT == kOutIdent) IH[r] = DH[r] = IE[r] = DE[r] = 0u;
     }
     uint32_t hdiag = pack2b(edge_h(rowA, go, ge, LOCAL), edge_h(rowB, go, ge, LOCAL));
     uint32_t outH = kBias2, outF = kNeg2;
+    // Identity: counts of the diagonal H and of the bottom row's H and F.
+    uint32_t gdI = 0u, gdD = 0u, outIH = 0u, outDH = 0u, outIF = 0u, outDF = 0u;
+    (void)gdI, (void)gdD, (void)outIH, (void)outDH, (void)outIF, (void)outDF;
+    // Traceback: plane words of this lane at step 0 of bands 2p and 2p+1
+    // (band B's step index is s - G); a step adds G words.
+    const int nS = n + G - 1;
+    const int64_t wordA = ((int64_t)(2 * pass) * nS) * G + t;
+    const int64_t wordB = ((int64_t)(2 * pass + 1) * nS - G) * G + t;
+    const bool hasB = 2 * pass + 1 < nbands;
+    (void)nS, (void)wordA, (void)wordB, (void)hasB;
 
     cp_async_wait_all();
     __syncwarp();
-    stage_chunk_rt<uint32_t, kCodeRing16>(G, 0, t, nact, top, top_ring, A.ccodes, boff, code_ring);
+    stage_chunk_rt<Top, kCodeRing16>(G, 0, t, nact, top, top_ring, A.ccodes, boff, code_ring);
     cp_async_commit();
     cp_async_wait_all();
     __syncwarp();
-    stage_chunk_rt<uint32_t, kCodeRing16>(G, 1, t, nact, top, top_ring, A.ccodes, boff, code_ring);
+    stage_chunk_rt<Top, kCodeRing16>(G, 1, t, nact, top, top_ring, A.ccodes, boff, code_ring);
     cp_async_commit();
 
     uint2 pa[2], pb[2];
-    uint32_t tv[2];
+    Top tv[2];
+    uint32_t ma[2] = {0u, 0u}, mb[2] = {0u, 0u};  // identity: match words of the columns
+    (void)ma, (void)mb;
     {
       const int ca = code_ring[(boff - t) & (kCodeRing16 - 1)];
       const int cb = code_ring[(boff - t - G) & (kCodeRing16 - 1)];
       pa[0] = profA[(2 * ca) * kThreads16];
       pb[0] = profB[(2 * cb) * kThreads16];
+      if constexpr (OUT == kOutIdent) {
+        ma[0] = s_match[ca * kThreads16 + threadIdx.x];
+        mb[0] = s_match[cb * kThreads16 + threadIdx.x];
+      }
       tv[0] = top_ring[0];
     }
 
@@ -304,7 +423,7 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
     const int cA0 = int(boff & (kCodeRing16 - 1)) - t + 1 + kCodeRing16;  // code of column jA + 1, positive
     const int cB0 = cA0 - G;                                               // code of column jB + 1
     auto step = [&](const int s, auto k_tag, auto interior_tag, auto last_tag, const uint8_t *codeA,
-                    const uint8_t *codeB, const uint32_t *topp) {
+                    const uint8_t *codeB, const Top *topp) {
       constexpr int k = decltype(k_tag)::value;
       constexpr int cur = k & 1, nxt = cur ^ 1;
       constexpr bool INTERIOR = decltype(interior_tag)::value;
@@ -313,37 +432,69 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       if (decltype(last_tag)::value && ((s + 1) & (kChunk - 1)) == 0) {
         cp_async_wait_all();
         __syncwarp();
-        stage_chunk_rt<uint32_t, kCodeRing16>(G, (s + 1) / kChunk + 1, t, nact, top, top_ring, A.ccodes, boff,
+        stage_chunk_rt<Top, kCodeRing16>(G, (s + 1) / kChunk + 1, t, nact, top, top_ring, A.ccodes, boff,
                                               code_ring);
         cp_async_commit();
       }
       const uint32_t rH = __shfl_sync(0xffffffffu, outH, src_lane);
       const uint32_t rF = __shfl_sync(0xffffffffu, outF, src_lane);
+      uint32_t rIH = 0u, rDH = 0u, rIF = 0u, rDF = 0u;
+      (void)rIH, (void)rDH, (void)rIF, (void)rDF;
+      if constexpr (OUT == kOutIdent) {
+        rIH = __shfl_sync(0xffffffffu, outIH, src_lane);
+        rDH = __shfl_sync(0xffffffffu, outDH, src_lane);
+        rIF = __shfl_sync(0xffffffffu, outIF, src_lane);
+        rDF = __shfl_sync(0xffffffffu, outDF, src_lane);
+      }
       const int jA = s - t, jB = jA - G;
       const uint2 wa = pa[cur], wb = pb[cur];
+      uint32_t mw = 0u;  // identity: match bits of this step's columns
+      (void)mw;
+      if constexpr (OUT == kOutIdent) mw = (ma[cur] & 0x0000FFFFu) | (mb[cur] & 0xFFFF0000u);
       {
         const int ca = codeA[k];
         const int cb = codeB[k];
         pa[nxt] = profA[(2 * ca) * kThreads16];
         pb[nxt] = profB[(2 * cb) * kThreads16];
+        if constexpr (OUT == kOutIdent) {
+          ma[nxt] = s_match[ca * kThreads16 + threadIdx.x];
+          mb[nxt] = s_match[cb * kThreads16 + threadIdx.x];
+        }
       }
       // Lane 0: band A from the staged top row, band B from lane G-1's
       // band-A bottom; other lanes take the shuffled values whole.  Lane-
       // dependent PRMT selectors instead of a branch; every lane of a group
       // reads lane 0's ring entry (one broadcast address per group).
-      const uint32_t upH = prmt(tv[cur], rH, selH);
-      const uint32_t upF = prmt(tv[cur], rF, selF);
+      const uint32_t upH = prmt(top_hf(tv[cur]), rH, selH);
+      const uint32_t upF = prmt(top_hf(tv[cur]), rF, selF);
+      uint32_t upIH = 0u, upDH = 0u, upIF = 0u, upDF = 0u;
+      if constexpr (OUT == kOutIdent) {
+        // Ring entry: (I, D) of H in .y, of F in .z.
+        upIH = prmt(tv[cur].y, rIH, selH);
+        upDH = prmt(tv[cur].y, rDH, selF);
+        upIF = prmt(tv[cur].z, rIF, selH);
+        upDF = prmt(tv[cur].z, rDF, selF);
+      }
       tv[nxt] = topp[k];
       const bool vA = INTERIOR || (unsigned)jA < (unsigned)nact;
       const bool vB = INTERIOR || (unsigned)jB < (unsigned)nact;
       if (vA || vB) {
         uint32_t d = hdiag;
-        // F of the lane's first row from the row above it.
+        // F of the lane's first row from the row above it: max(F - ext,
+        // H - open - ext) with the true H above.
         // (In the interior every upH is a real cell, far above the floor, so
         // the subtraction runs as an IMAD on the FMA pipe.)
-        uint32_t fv = __viaddmax_u16x2(upF, nge2,
-                                       INTERIOR ? sub2_imad(upH, one, neg_oe2) : __viaddmax_u16x2(upH, noe2, kNeg2));
+        const uint32_t xo0 = INTERIOR ? sub2_imad(upH, one, neg_oe2) : __viaddmax_u16x2(upH, noe2, kNeg2);
+        uint32_t fv = __viaddmax_u16x2(upF, nge2, xo0);
         uint32_t xo = 0u;
+        // Traceback: the nibbles of rows 0-3 and 4-7 (12 in each nibble
+        // stands for both opened; the decisions subtract from it).
+        uint32_t acc1 = 0xCCCCCCCCu, acc2 = 0xCCCCCCCCu;
+        uint32_t nz1 = 0u, nz2w = 0u;  // local: rows whose H is above 0
+        // Identity: counts of the cell above (H and F) and of the diagonal.
+        uint32_t ciH = upIH, cdH = upDH, ciF = upIF, cdF = upDF;
+        uint32_t gI = gdI, gD = gdD;
+        (void)acc1, (void)acc2, (void)nz1, (void)nz2w, (void)ciH, (void)cdH, (void)ciF, (void)cdF, (void)gI, (void)gD;
         // Rows in order.  Since open >= 0, F(i+1,j) = max(F(i,j) - ext,
         // max(X(i,j) [, 0]) - open - ext) with X = max(D + s, E): the only
         // dependence between rows is one add-max on F.
@@ -353,11 +504,73 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
           for (int r = 0; r < R; ++r) {
             const uint32_t sc = score2_dyn(r < 4 ? wa.x : wa.y, r < 4 ? wb.x : wb.y, r);
             uint32_t e = __viaddmax_u16x2(E[r], nge2, T[r]);
-            const uint32_t x = __viaddmax_u16x2(d, sc, e);
+            uint32_t x, dd = 0u;
+            (void)dd;
+            if constexpr (OUT == kOutScore) {
+              x = __viaddmax_u16x2(d, sc, e);
+            } else {
+              dd = __viaddmax_u16x2(d, sc, 0u);  // D + s per half
+              x = __vimax3_u16x2(dd, e, e);
+            }
+            const uint32_t fo = r == 0 ? xo0 : xo;  // F's open candidate
             const uint32_t f = r == 0 ? fv : __viaddmax_u16x2(fv, nge2, xo);
             uint32_t h = LOCAL ? __vimax3_u16x2(x, f, kBias2) : __vimax3_u16x2(x, f, f);
             uint32_t tn = sub2_imad(h, one, neg_oe2);
             xo = LOCAL ? __viaddmax_u16x2(x, noe2, zero_oe2) : sub2_imad(x, one, neg_oe2);
+            (void)fo;
+            if constexpr (OUT == kOutTrace) {
+              // dir = [h > dd] + [h > x]; bits 2 and 3 clear when E / F
+              // extended.
+              uint32_t c = imad(nz2(h, x, minus_one, k1), one, nz2(h, dd, minus_one, k1));
+              c = imad(nz2(e, T[r], minus_one, k1), m4, c);
+              c = imad(nz2(f, fo, minus_one, k1), m8, c);
+              const uint32_t w = (r & 3) == 0 ? one : (r & 3) == 1 ? k16 : (r & 3) == 2 ? k256 : k4096;
+              if (r < 4)
+                acc1 = imad(c, w, acc1);
+              else
+                acc2 = imad(c, w, acc2);
+              if constexpr (LOCAL) {
+                const uint32_t z = nz2(h, kBias2, minus_one, k1);
+                if (r < 4)
+                  nz1 = imad(z, w, nz1);
+                else
+                  nz2w = imad(z, w, nz2w);
+              }
+            }
+            if constexpr (OUT == kOutIdent) {
+              // Masks (0xFFFF per half): E extended, F extended, X from E,
+              // H from F.
+              const uint32_t mE = imad(nz2(e, T[r], minus_one, k1), kffff, 0u);
+              const uint32_t mF = imad(nz2(f, fo, minus_one, k1), kffff, 0u);
+              const uint32_t mX = imad(nz2(x, dd, minus_one, k1), kffff, 0u);
+              const uint32_t mH = imad(nz2(h, x, minus_one, k1), kffff, 0u);
+              uint32_t ie = (IE[r] & mE) | (IH[r] & ~mE);
+              uint32_t de = (DE[r] & mE) | (DH[r] & ~mE);
+              const uint32_t iF = (ciF & mF) | (ciH & ~mF);
+              const uint32_t dF = (cdF & mF) | (cdH & ~mF);
+              // Diagonal: + match bit of row r (bit r, bit 16 + r of mw),
+              // + 1 diagonal column in each half.
+              const uint32_t id = imad((mw >> r) & 0x00010001u, one, gI);
+              const uint32_t dg = imad(k1, one, gD);
+              uint32_t ih = (((ie & mX) | (id & ~mX)) & ~mH) | (iF & mH);
+              uint32_t dh = (((de & mX) | (dg & ~mX)) & ~mH) | (dF & mH);
+              if constexpr (MASKED) {
+                ih = (ih & ~keep) | (IH[r] & keep);
+                dh = (dh & ~keep) | (DH[r] & keep);
+                ie = (ie & ~keep) | (IE[r] & keep);
+                de = (de & ~keep) | (DE[r] & keep);
+              }
+              gI = IH[r];
+              gD = DH[r];
+              IH[r] = ih;
+              DH[r] = dh;
+              IE[r] = ie;
+              DE[r] = de;
+              ciH = ih;
+              cdH = dh;
+              ciF = iF;
+              cdF = dF;
+            }
             if constexpr (MASKED) {
               h = (h & ~keep) | (H[r] & keep);
               tn = (tn & ~keep) | (T[r] & keep);
@@ -365,11 +578,20 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
             }
             if constexpr (CHECK) hmax = __vimax3_u16x2(hmax, h, h);
             if constexpr (LOCAL) {
-              // Halves where this cell beats the row's best so far
-              // (strictly, so the first column of a maximum is kept).
-              const uint32_t cm = __vcmpgtu2(h, best[r]);
-              best[r] = __vimax3_u16x2(best[r], h, h);
-              bcol[r] = (bcol[r] & ~cm) | (pack2(jA + 1, jB + 1) & cm);
+              if constexpr (OUT == kOutScore) {
+                // Halves where this cell beats the row's best so far
+                // (strictly, so the first column of a maximum is kept).
+                const uint32_t cm = __vcmpgtu2(h, best[r]);
+                best[r] = __vimax3_u16x2(best[r], h, h);
+                bcol[r] = (bcol[r] & ~cm) | (pack2(jA + 1, jB + 1) & cm);
+              } else {
+                // The same with the decision arithmetic: the new best
+                // differs from the old one exactly where h beat it.
+                const uint32_t nb = __vimax3_u16x2(best[r], h, h);
+                const uint32_t cm = imad(nz2(nb, best[r], minus_one, k1), kffff, 0u);
+                best[r] = nb;
+                bcol[r] = (bcol[r] & ~cm) | (pack2(jA + 1, jB + 1) & cm);
+              }
             }
             d = H[r];
             H[r] = h;
@@ -378,41 +600,90 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
             fv = f;
           }
         };
-        if (INTERIOR || (vA && vB)) {
+        // (Outside the interior the traceback and identity fills run the
+        // masked sweep alone, whose keep mask is 0 when both halves are in
+        // range: their sweeps are large, and fewer copies of them keep the
+        // kernel within the instruction cache.)
+        if (INTERIOR || (OUT == kOutScore && vA && vB)) {
           hdiag = upH;
+          if constexpr (OUT == kOutIdent) {
+            gdI = upIH;
+            gdD = upDH;
+          }
           sweep(BoolTag<false>{}, 0u);
         } else {
           // Halves outside their column range keep their old values; a
           // half that has not started keeps its left-boundary diagonal.
-          const uint32_t keep = vA ? 0xFFFF0000u : 0x0000FFFFu;
+          const uint32_t keep = (vA ? 0u : 0x0000FFFFu) | (vB ? 0u : 0xFFFF0000u);
           hdiag = (upH & ~keep) | (hdiag & keep);
+          if constexpr (OUT == kOutIdent) {
+            gdI = (upIH & ~keep) | (gdI & keep);
+            gdD = (upDH & ~keep) | (gdD & keep);
+          }
           sweep(BoolTag<true>{}, keep);
         }
         outH = H[R - 1];
         outF = fv;
-        if (t == G - 1 && vB) top[jB] = prmt(outH, outF, 0x7632u);
+        if constexpr (OUT == kOutIdent) {
+          outIH = IH[R - 1];
+          outDH = DH[R - 1];
+          outIF = ciF;
+          outDF = cdF;
+          if (t == G - 1 && vB)
+            top[jB] = make_uint4(prmt(outH, outF, 0x7632u), prmt(outIH, outDH, 0x7632u),
+                                 prmt(outIF, outDF, 0x7632u), 0u);
+        } else {
+          if (t == G - 1 && vB) top[jB] = prmt(outH, outF, 0x7632u);
+        }
+        if constexpr (OUT == kOutTrace) {
+          if constexpr (LOCAL) {
+            // A local stop (H = 0) has direction 3.
+            acc1 |= (0x11111111u - nz1) * 3u;
+            acc2 |= (0x11111111u - nz2w) * 3u;
+          }
+          if (vA) planes[wordA + (int64_t)s * G] = prmt(acc1, acc2, 0x5410u);
+          if (vB && hasB) planes[wordB + (int64_t)s * G] = prmt(acc1, acc2, 0x7632u);
+        }
       }
     };
     int s0 = 0;
     auto pair_of_steps = [&]() {
       const uint8_t *codeA = code_ring + ((cA0 + s0) & (kCodeRing16 - 1));
       const uint8_t *codeB = code_ring + ((cB0 + s0) & (kCodeRing16 - 1));
-      const uint32_t *topp = top_ring + ((s0 + 1) & (kTopRing - 1));
+      const Top *topp = top_ring + ((s0 + 1) & (kTopRing - 1));
       step(s0, IntTag<0>{}, BoolTag<false>{}, BoolTag<false>{}, codeA, codeB, topp);
       step(s0 + 1, IntTag<1>{}, BoolTag<false>{}, BoolTag<true>{}, codeA, codeB, topp);
     };
     auto quad_of_steps = [&]() {
       const uint8_t *codeA = code_ring + ((cA0 + s0) & (kCodeRing16 - 1));
       const uint8_t *codeB = code_ring + ((cB0 + s0) & (kCodeRing16 - 1));
-      const uint32_t *topp = top_ring + ((s0 + 1) & (kTopRing - 1));
+      const Top *topp = top_ring + ((s0 + 1) & (kTopRing - 1));
       step(s0, IntTag<0>{}, BoolTag<true>{}, BoolTag<false>{}, codeA, codeB, topp);
       step(s0 + 1, IntTag<1>{}, BoolTag<true>{}, BoolTag<false>{}, codeA, codeB, topp);
       step(s0 + 2, IntTag<2>{}, BoolTag<true>{}, BoolTag<false>{}, codeA, codeB, topp);
       step(s0 + 3, IntTag<3>{}, BoolTag<true>{}, BoolTag<true>{}, codeA, codeB, topp);
     };
-    for (; s0 < i0; s0 += 2) pair_of_steps();
-    for (; s0 < i1; s0 += 4) quad_of_steps();
-    for (; s0 < steps_pad; s0 += 2) pair_of_steps();
+    if constexpr (OUT == kOutScore) {
+      for (; s0 < i0; s0 += 2) pair_of_steps();
+      for (; s0 < i1; s0 += 4) quad_of_steps();
+      for (; s0 < steps_pad; s0 += 2) pair_of_steps();
+    } else {
+      // Traceback and identity: units of two steps in the interior too
+      // (code size, as above).
+      auto pair_interior = [&]() {
+        const uint8_t *codeA = code_ring + ((cA0 + s0) & (kCodeRing16 - 1));
+        const uint8_t *codeB = code_ring + ((cB0 + s0) & (kCodeRing16 - 1));
+        const Top *topp = top_ring + ((s0 + 1) & (kTopRing - 1));
+        step(s0, IntTag<0>{}, BoolTag<true>{}, BoolTag<false>{}, codeA, codeB, topp);
+        step(s0 + 1, IntTag<1>{}, BoolTag<true>{}, BoolTag<true>{}, codeA, codeB, topp);
+      };
+#pragma unroll 1
+      for (; s0 < i0; s0 += 2) pair_of_steps();
+#pragma unroll 1
+      for (; s0 < i1; s0 += 2) pair_interior();
+#pragma unroll 1
+      for (; s0 < steps_pad; s0 += 2) pair_of_steps();
+    }
     cp_async_wait_all();
     __syncwarp();
 
@@ -440,7 +711,13 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
         const int lr = (w - half * P) - t * R;
 #pragma unroll
         for (int r = 0; r < R; ++r)
-          if (r == lr) last_h = half ? hi16b(H[r]) : lo16b(H[r]);
+          if (r == lr) {
+            last_h = half ? hi16b(H[r]) : lo16b(H[r]);
+            if constexpr (OUT == kOutIdent) {
+              last_i = half ? IH[r] >> 16 : IH[r] & 0xFFFFu;
+              last_d = half ? DH[r] >> 16 : DH[r] & 0xFFFFu;
+            }
+          }
       }
     }
   }
@@ -474,6 +751,11 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       owner = (w % P) / R;
     }
     const int32_t h = __shfl_sync(0xffffffffu, last_h, gw * G + owner);
+    uint32_t ci = 0u, cd = 0u;
+    if constexpr (OUT == kOutIdent) {
+      ci = __shfl_sync(0xffffffffu, last_i, gw * G + owner);
+      cd = __shfl_sync(0xffffffffu, last_d, gw * G + owner);
+    }
     if (have && t == 0) {
       ResultDev &o = A.res[pid];
       o.status = gbad ? TSQ_E_INVALID_RESIDUE : TSQ_OK;
@@ -482,21 +764,42 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
       o.b_begin = 0;
       o.b_end = n;
       o.score = (m == 0 || n == 0) ? ((m + n == 0) ? 0 : -(go + (m + n) * ge)) : h;
-      o.n_ident = o.n_cols = -1;
+      if (OUT != kOutScore && (m == 0 || n == 0)) {
+        o.n_ident = 0;
+        o.n_cols = m + n;
+      } else if (OUT == kOutIdent) {
+        o.n_ident = int32_t(ci);
+        o.n_cols = m + n - int32_t(cd);
+      } else {
+        o.n_ident = o.n_cols = -1;
+      }
       if (CHECK) A.overflow[pid] = goverflow ? 1 : 0;
     }
   }
   __syncwarp();
 }
 
-template <bool LOCAL, bool CHECK>
+// Shared memory of the int16x2 fills: class matrix, per-thread profile
+// (two words of 8 rows per class), identity's match table, group rings.
+__host__ __device__ constexpr size_t smem16_prof_bytes(int nclasses) {
+  return size_t(2 * nclasses) * kThreads16 * sizeof(uint2);
+}
+__host__ __device__ constexpr size_t smem16_match_bytes(int out_mode, int nclasses) {
+  return out_mode == kOutIdent ? size_t(nclasses) * kThreads16 * sizeof(uint32_t) : 0;
+}
+__host__ __device__ constexpr size_t smem16_top_stride(int out_mode) {
+  return size_t(kTopRing) * (out_mode == kOutIdent ? 16 : 4) + kRingPad;
+}
+
+template <bool LOCAL, bool CHECK, int OUT>
 __global__ void __launch_bounds__(kThreads16) fill_i16_kernel(const FillArgs A) {
   extern __shared__ __align__(16) uint8_t smem[];
   // Class scores, one 32-byte row per class, then a zero row (index
   // nclasses) for padding rows.
   int8_t *s_mat = reinterpret_cast<int8_t *>(smem);
   uint2 *s_prof = reinterpret_cast<uint2 *>(smem + kMatBytes16);
-  uint8_t *s_rings = smem + kMatBytes16 + size_t(2 * A.nclasses) * kThreads16 * sizeof(uint2);
+  uint32_t *s_match = reinterpret_cast<uint32_t *>(smem + kMatBytes16 + smem16_prof_bytes(A.nclasses));
+  uint8_t *s_rings = smem + kMatBytes16 + smem16_prof_bytes(A.nclasses) + smem16_match_bytes(OUT, A.nclasses);
   for (int k = threadIdx.x; k < kMatBytes16; k += blockDim.x) {
     const int x = k / kMatRow16, c = k % kMatRow16;
     s_mat[k] = (x < A.nclasses && c < A.nclasses) ? A.cmatrix[x * A.nclasses + c] : int8_t(0);
@@ -505,7 +808,7 @@ __global__ void __launch_bounds__(kThreads16) fill_i16_kernel(const FillArgs A) 
   // ring, and the step uses what it reads as a profile index unchecked
   // (every class code the rings receive is below nclasses).
   {
-    uint8_t *code_rings = s_rings + kSlots16 * (kTopRing * 4 + kRingPad);
+    uint8_t *code_rings = s_rings + kSlots16 * smem16_top_stride(OUT);
     for (int k = threadIdx.x; k < kSlots16 * (kCodeRing16 + kRingPad); k += blockDim.x) code_rings[k] = 0;
   }
   __syncthreads();
@@ -520,8 +823,58 @@ __global__ void __launch_bounds__(kThreads16) fill_i16_kernel(const FillArgs A) 
     const int2 w = A.wtasks[idx];
     const int G = w.y >> 16, count = w.y & 0xFFFF;
     const int lg = G == 4 ? 2 : (G == 8 ? 3 : (G == 16 ? 4 : 5));
-    fill16_warp_task<LOCAL, CHECK>(A, s_mat, s_prof, s_rings, w.x, count, warp_id, 1 << lg, lg);
+    fill16_warp_task<LOCAL, CHECK, OUT>(A, s_mat, s_prof, s_match, s_rings, w.x, count, warp_id, 1 << lg, lg);
   }
+}
+
+size_t smem_i16(int out_mode, int nclasses);
+
+// Launch and residency of the int16x2 fill of one output mode (each mode
+// is instantiated in its own translation unit).
+template <int OUT>
+cudaError_t launch_i16(bool check, bool local, const FillArgs &args, int blocks, size_t smem, cudaStream_t st) {
+  FillArgs a = args;
+  a.one = 1u;
+  if constexpr (OUT == kOutIdent) {
+    if (local) return cudaErrorInvalidValue;
+    if (check)
+      fill_i16_kernel<false, true, OUT><<<blocks, kThreads16, smem, st>>>(a);
+    else
+      fill_i16_kernel<false, false, OUT><<<blocks, kThreads16, smem, st>>>(a);
+  } else {
+    if (check) {
+      if (local)
+        fill_i16_kernel<true, true, OUT><<<blocks, kThreads16, smem, st>>>(a);
+      else
+        fill_i16_kernel<false, true, OUT><<<blocks, kThreads16, smem, st>>>(a);
+    } else {
+      if (local)
+        fill_i16_kernel<true, false, OUT><<<blocks, kThreads16, smem, st>>>(a);
+      else
+        fill_i16_kernel<false, false, OUT><<<blocks, kThreads16, smem, st>>>(a);
+    }
+  }
+  return cudaGetLastError();
+}
+
+template <int OUT>
+int occupancy_i16(bool check, bool local, size_t smem) {
+  void (*k)(const FillArgs);
+  if constexpr (OUT == kOutIdent) {
+    if (local) return 0;
+    k = check ? fill_i16_kernel<false, true, OUT> : fill_i16_kernel<false, false, OUT>;
+  } else {
+    k = check ? (local ? fill_i16_kernel<true, true, OUT> : fill_i16_kernel<false, true, OUT>)
+              : (local ? fill_i16_kernel<true, false, OUT> : fill_i16_kernel<false, false, OUT>);
+  }
+  // The attribute allows the largest profile (26 classes), so that every
+  // scheme's launch fits whatever scheme was sized first.
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           int(std::max(smem, smem_i16(OUT, kLetters)))) != cudaSuccess)
+    return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kThreads16, smem) != cudaSuccess) return 0;
+  return nb;
 }
 
 }  // namespace fill

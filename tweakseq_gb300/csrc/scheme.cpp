@@ -55,7 +55,9 @@ int blosum_row(char letter) {
   return p ? int(p - kRowOrder) : -1;
 }
 
-void finish(Scheme *s) {
+// letters: every valid letter its own class (identity fills test letter
+// equality on class codes).
+void finish(Scheme *s, bool letters) {
   s->max_score = -128;
   s->min_score = 127;
   s->symmetric = true;
@@ -68,13 +70,14 @@ void finish(Scheme *s) {
       if (s->score[x][y] != s->score[y][x]) s->symmetric = false;
     }
   if (s->max_score < s->min_score) s->max_score = s->min_score = 0;
-  // Score classes, numbered in letter order of their first letter.
+  // Score classes, numbered in letter order of their first letter (or of
+  // their only letter).
   int rep[kLetters];
   s->nclasses = 0;
   for (int x = 0; x < kLetters; ++x) {
     s->cls[x] = kBadCode;
     if (!s->valid[x]) continue;
-    for (int c = 0; c < s->nclasses && s->cls[x] == kBadCode; ++c) {
+    for (int c = 0; !letters && c < s->nclasses && s->cls[x] == kBadCode; ++c) {
       const int r = rep[c];
       bool same = true;
       for (int y = 0; y < kLetters && same; ++y)
@@ -119,7 +122,7 @@ int build_scheme(const tsq_params *p, Scheme *out) {
     default:
       return TSQ_E_INVALID_ARG;
   }
-  finish(out);
+  finish(out, p->output == TSQ_OUT_IDENTITY);
   return TSQ_OK;
 }
 

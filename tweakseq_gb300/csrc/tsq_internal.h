@@ -41,8 +41,9 @@ struct Scheme {
   int32_t max_score, min_score;
   bool symmetric;
   // Score classes: valid letters with the same row and column of scores
-  // (BLOSUM62: J, O, U and X) share a class; the int16x2 score fill indexes
-  // its profile by class, which keeps the profile small.
+  // (BLOSUM62: J, O, U and X) share a class; the int16x2 fills index their
+  // profile by class, which keeps the profile small.  For identity output
+  // every valid letter is its own class (identical = same class).
   int32_t nclasses;
   uint8_t cls[kLetters];               // class of each letter, kBadCode if invalid
   int8_t cscore[kLetters * kLetters];  // nclasses x nclasses class scores

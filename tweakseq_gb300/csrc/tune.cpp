@@ -180,10 +180,10 @@ extern "C" int tsq_tune_run(const char *json_path, int32_t quick) {
         bool free;
       };
       std::vector<Cand> cands;
-      cands.push_back(Cand{4, out == kOutScore ? 1 : 0, 0, true});
+      cands.push_back(Cand{4, 1, 0, true});
       for (int G : kWidths) {
         cands.push_back(Cand{G, 0, 0, false});
-        if (out == kOutScore) cands.push_back(Cand{G, 1, 0, false});
+        cands.push_back(Cand{G, 1, 0, false});
       }
       if (kEdges[bk] >= kCtaFrom) cands.push_back(Cand{32, 0, 1, false});
       Entry best{out, kEdges[bk], kEdges[bk + 1], Shape{32, 8, 0}, 0, 0.0};
