@@ -62,7 +62,10 @@ def parse_args():
     ap.add_argument("--no-configs", action="store_true", help="skip the other configurations")
     ap.add_argument("--configs-only", action="store_true", help="run only the other configurations")
     ap.add_argument("--msa-only", action="store_true", help="run only the consensus and guide-tree legs")
-    ap.add_argument("--profile-case", choices=["long_dna", "identity", "consensus", "uniform"], default=None,
+    ap.add_argument("--profile-lane", choices=["auto", "i16", "i32"], default="auto",
+                    help="lane type of the --profile-case batch")
+    ap.add_argument("--profile-case", choices=["long_dna", "identity", "consensus", "uniform", "traceback"],
+                    default=None,
                     help="small profiling case of another kernel (for ncu)")
     return ap.parse_args()
 
@@ -573,6 +576,11 @@ def configs_leg(c3_pairs=12):
         "pairs": len(ps), "cells": ps.cells, "output": "alignment (global, BLOSUM62 11/1)",
         "batched_gcups": ps.cells / (float(np.median(ms)) * 1e-3) / 1e9, "e2e_gcups": ps.cells / e2e_s / 1e9,
         "plain_gcups": ps.cells / plain_s / 1e9, "mismatches_vs_oracle": mism}
+    # Full traceback on the headline's 100,000 uneven pairs: the int16x2
+    # traceback fill (planes in HBM) and the walker, device-resident, next
+    # to the same batch on int32 lanes; strings of a seeded sample against
+    # the oracle.
+    out["traceback_uneven_pairs_100k"] = traceback_uneven(O, A, W, cores)
     # All 1,000 long DNA pairs with traceback through tsq_align_batch,
     # which runs them in waves sized to the free HBM (their planes need about
     # 500 GB), checked against the oracle on a seeded sample of pairs.
@@ -641,9 +649,15 @@ def configs_leg(c3_pairs=12):
     sub = ps.subset(idx)
     want = O.batch(sub.seqs, sub.a_off, sub.a_len, sub.b_off, sub.b_len, mode=O.MODE_IDENT, nthreads=cores)
     mism = int(sum((res.table[f][idx] != want[f]).sum() for f in ("score", "n_ident", "n_cols")))
+    # The same batch on int32 lanes only (the int32 identity fill), for
+    # comparison with the int16x2 identity fill the planner picks.
+    with A.Batch(ps, output="identity", use_graph=True, lane="i32") as b:
+        b.run()
+        b.run()
+        st_i32 = b.stats()
     fill_gcups = ps.cells / (st["fill_ms"] * 1e-3) / 1e9
-    peak = dpx_cell_peak(False)
-    rec = traffic_record("fill_i32_identity_guide_tree_200k")
+    peak = dpx_cell_peak(True)
+    rec = traffic_record("fill_i16_identity_guide_tree_200k")
     traffic = rec["dram_bytes_per_launch"] * len(ps) / rec["pairs"] if rec else None
     # The plain per-pair path on a sample of the same pairs.
     plain_idx = np.random.default_rng(6).choice(len(ps), 300, replace=False)
@@ -659,19 +673,77 @@ def configs_leg(c3_pairs=12):
         "plain_gcups": plain_cells / plain_s / 1e9, "plain_pairs": len(plain_idx),
         "autotune": {"tune_s": tune_s, "identity_buckets": tuned_entries,
                      "untuned_fill_gcups": ps.cells / (st_untuned["fill_ms"] * 1e-3) / 1e9},
-        "roofline": {"bound": "int", "kernel": "fill_i32_kernel (identity, global)", "achieved": fill_gcups,
+        "int32_lanes_fill_gcups": ps.cells / (st_i32["fill_ms"] * 1e-3) / 1e9,
+        "roofline": {"bound": "int", "kernel": "fill_i16_kernel (identity, global)", "achieved": fill_gcups,
                      "peak": peak, "unit": "Gcell/s", "frac": fill_gcups / peak, "traffic": traffic,
                      "traffic_source": "ncu DRAM bytes of a 200,000-pair launch, scaled by pairs",
-                     "peak_source": "measured live: tsq_probe_dpx int32 rate / 4 DPX instructions per cell"},
+                     "peak_source": "measured live: tsq_probe_dpx int16x2 rate x 2 cells / 4 DPX instructions "
+                                    "per cell (the recurrence's four maxima; the identity fill also issues the "
+                                    "path-count decisions and selects)"},
         "mismatches_vs_oracle": mism, "checked": "4,000 seeded pairs"}
     return out
 
 
-def long_pair_kernels(ps, n_pairs=64):
+def traceback_uneven(O, A, W, cores, sample=2000):
+    ps = W.uneven_pairs()
+    runs = {}
+    for lane in ("auto", "i32"):
+        fills, devs = [], []
+        with A.Batch(ps, output="alignment", use_graph=True, lane=lane) as b:
+            b.run()
+            for _ in range(3):
+                b.run()
+                st = b.stats()
+                fills.append(st["fill_ms"])
+                devs.append(st["device_ms"])
+            res = b.results() if lane == "auto" else None
+        runs[lane] = (float(np.median(fills)), float(np.median(devs)), res)
+    fill_ms, dev_ms, res = runs["auto"]
+    idx = np.sort(np.random.default_rng(8).choice(len(ps), sample, replace=False))
+    sub = ps.subset(idx)
+    want, sa, sb = O.batch(sub.seqs, sub.a_off, sub.a_len, sub.b_off, sub.b_len, mode=O.MODE_ALIGN, strings=True,
+                           nthreads=cores)
+    fields = ("score", "a_begin", "a_end", "b_begin", "b_end", "n_ident", "n_cols")
+    mism = int(sum((res.table[f][idx] != want[f]).sum() for f in fields))
+    mism += sum(res.aln_a[k] != sa[j] or res.aln_b[k] != sb[j] for j, k in enumerate(idx))
+    gc = ps.cells / (fill_ms * 1e-3) / 1e9
+    peak = dpx_cell_peak(True)
+    hbm, hbm_src = hbm_peak()
+    plane_gbs = 0.5 * ps.cells / (fill_ms * 1e-3) / 1e9
+    rec = traffic_record("fill_i16_traceback_uneven_20k")
+    traffic = rec["dram_bytes_per_launch"] * ps.cells / rec["cells"] if rec else None
+    return {
+        "pairs": len(ps), "cells": ps.cells, "output": "alignment (global, BLOSUM62 11/1)",
+        "fill_gcups": gc, "device_gcups": ps.cells / (dev_ms * 1e-3) / 1e9,
+        "int32_lanes_fill_gcups": ps.cells / (runs["i32"][0] * 1e-3) / 1e9,
+        "int32_lanes_device_gcups": ps.cells / (runs["i32"][1] * 1e-3) / 1e9,
+        "roofline": {"bound": "int", "kernel": "fill_i16_kernel (traceback, global)", "achieved": gc, "peak": peak,
+                     "unit": "Gcell/s", "frac": gc / peak, "traffic": traffic,
+                     "traffic_source": "ncu DRAM bytes of a 20,000-pair launch, scaled by cells",
+                     "peak_source": "measured live: tsq_probe_dpx int16x2 rate x 2 cells / 4 DPX instructions "
+                                    "per cell (the recurrence's four maxima; the traceback fill also issues the "
+                                    "decision bits)"},
+        "plane_writes": {"bound": "hbm", "achieved": plane_gbs, "peak": hbm, "unit": "GB/s", "frac": plane_gbs / hbm,
+                         "bytes_per_cell": 0.5, "peak_source": hbm_src},
+        "mismatches_vs_oracle": mism,
+        "checked": f"{sample} seeded pairs byte for byte: score, coordinates, identity, both gapped strings"}
+
+
+def long_pair_kernels(ps, per_sm=2):
     """Rooflines of the long-pair kernels: a device-resident batch of the
-    first n_pairs long DNA pairs (one CTA per pair: the CTA traceback fill,
-    then one walker warp per pair), timed by the batch's own events."""
+    first long DNA pairs, per_sm of them per SM (the CTA fill's residency,
+    so that every SM holds that many pairs at once) as far as their
+    traceback planes fit in 40 % of the free HBM (at most 120 GB): the CTA
+    traceback fill, then one walker warp per pair, timed by the batch's own
+    events."""
+    import torch
+
     from tweakseq_gb300 import aligner as A
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    free = torch.cuda.mem_get_info()[0]
+    budget = min(120e9, 0.4 * free)
+    cells = np.cumsum(ps.a_len.astype(np.float64) * ps.b_len.astype(np.float64))
+    n_pairs = int(min(per_sm * sms, max(1, np.searchsorted(cells * 0.5, budget))))
     sub = ps.subset(np.arange(n_pairs))
     fills, rest = [], []
     with A.Batch(sub, matrix="dna", gap_open=5, gap_extend=2, output="alignment", use_graph=False) as b:
@@ -700,7 +772,8 @@ def long_pair_kernels(ps, n_pairs=64):
             "fill_ms": fill_s * 1e3,
             "roofline": {"bound": "int", "achieved": gc, "peak": peak, "unit": "Gcell/s", "frac": gc / peak,
                          "traffic": traffic, "traffic_source": "ncu DRAM bytes of a 32-pair launch, scaled by cells",
-                         "peak_source": "measured live: tsq_probe_dpx int32 rate / 4 DPX instructions per cell"},
+                         "peak_source": "measured live: tsq_probe_dpx int32 rate / 4 DPX instructions per cell",
+                         "note": f"{n_pairs} pairs, one CTA each, at most {per_sm} per SM"},
             "plane_writes": {"bound": "hbm", "achieved": plane_gbs, "peak": hbm, "unit": "GB/s",
                              "frac": plane_gbs / hbm, "bytes_per_cell": 0.5, "peak_source": hbm_src}},
         "walk_warp_kernel": {
@@ -808,8 +881,10 @@ def run_profile_case(args):
     """Small cases for ncu of the kernels behind the other measurements:
     long_dna (32 DNA pairs of 10-12 kb with traceback: the CTA fill and the
     walker),
-    identity (200,000 pairs of the guide-tree all-vs-all: the int32 identity
-    fill), consensus (100,000 x 2,000 alignment: the class-count kernel),
+    identity (200,000 pairs of the guide-tree all-vs-all: the identity
+    fill), traceback (20,000 of the uneven pairs with traceback: the
+    traceback fill and the walker), consensus (100,000 x 2,000 alignment:
+    the class-count kernel),
     uniform (20,000 protein pairs of 320 x 2,000: the int16x2 score fill with
     interior steps only, for instruction counts per step).
     Device-resident, no graph, warm-up then timed runs."""
@@ -822,7 +897,7 @@ def run_profile_case(args):
 
     B.build()
     case = args.profile_case
-    if case in ("long_dna", "identity", "uniform"):
+    if case in ("long_dna", "identity", "uniform", "traceback"):
         if case == "long_dna":
             ps = W.long_dna_pairs(32, lo=10_000, hi=12_000)
             kw = dict(matrix="dna", gap_open=5, gap_extend=2, output="alignment")
@@ -836,10 +911,14 @@ def run_profile_case(args):
                 pairs.append((2 * k, 2 * k + 1))
             ps = W._pairset_from_lists(seqs, pairs)
             kw = dict(output="score")
+        elif case == "traceback":
+            ps = W.uneven_pairs().subset(np.arange(20_000))
+            kw = dict(output="alignment")
         else:
             ps = W.guide_tree_families()
             ps = ps.subset(np.arange(200_000))
             kw = dict(output="identity")
+        kw["lane"] = args.profile_lane
         with A.Batch(ps, use_graph=False, **kw) as b:
             for _ in range(args.warmup + args.steps):
                 b.run()
