@@ -582,7 +582,8 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   // overflow-checked int16x2 kernel and are re-run in int32 if flagged;
   // everything else runs in int32.
   //
-  // Long int32 pairs go to the CTA fill (their bands striped over 8 warps):
+  // Long int32 pairs go to the CTA fill (their bands striped over the 16
+  // or 8 warps of a CTA):
   // those whose sweep on one 32-lane group -- ceil(m/256) bands of n+31
   // steps -- would outlast the batch's balanced per-lane work (or, alone,
   // 20,000 steps).

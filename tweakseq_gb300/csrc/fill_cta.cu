@@ -9,23 +9,27 @@ namespace tsq {
 namespace fill {
 
 namespace {
+template <bool LOCAL, int OUT>
+constexpr int kW = cta_warps(OUT, LOCAL);
+
 template <int OUT>
 cudaError_t go(bool local, const FillArgs &a, int blocks, cudaStream_t st) {
-  const size_t smem = cta_smem_bytes(OUT);
   if (local)
-    fill_cta_kernel<true, OUT><<<blocks, kCtaThreads, smem, st>>>(a);
+    fill_cta_kernel<true, OUT, kW<true, OUT>><<<blocks, kW<true, OUT> * 32, cta_smem_bytes(OUT, kW<true, OUT>), st>>>(a);
   else
-    fill_cta_kernel<false, OUT><<<blocks, kCtaThreads, smem, st>>>(a);
+    fill_cta_kernel<false, OUT, kW<false, OUT>>
+        <<<blocks, kW<false, OUT> * 32, cta_smem_bytes(OUT, kW<false, OUT>), st>>>(a);
   return cudaGetLastError();
 }
 
 template <int OUT>
 int occ(bool local) {
-  const size_t smem = cta_smem_bytes(OUT);
-  auto k = local ? fill_cta_kernel<true, OUT> : fill_cta_kernel<false, OUT>;
+  const int W = cta_warps(OUT, local);
+  const size_t smem = cta_smem_bytes(OUT, W);
+  auto k = local ? fill_cta_kernel<true, OUT, kW<true, OUT>> : fill_cta_kernel<false, OUT, kW<false, OUT>>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return 0;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kCtaThreads, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, W * 32, smem) != cudaSuccess) return 0;
   return nb;
 }
 }  // namespace

@@ -1,18 +1,21 @@
 // fill_cta.cuh -- one long pair per CTA: the pair's row bands are striped
-// over the CTA's 8 warps (band b runs on warp b mod 8), each warp a 32-lane
+// over the CTA's W warps (band b runs on warp b mod W), each warp a 32-lane
 // group of the int32 fill of fill_i32.cuh.  Consecutive bands run at the
 // same time, each a few chunks of columns behind the one above it, so a
-// pair of 50 kb sweeps with 8 warps instead of 1.
+// pair of 50 kb sweeps with W warps instead of 1.  W is 16 where the
+// kernel fits 128 registers (global score and traceback: one CTA fills an
+// SM's 16 warps with one pair, halving a long pair's time against two
+// 8-warp CTAs), 8 otherwise (local mode, identity).
 //
 // Band-to-band rows.  The bottom row of a band is the top row of the next.
-// Between warps w and w+1 (w < 7) it goes through a shared-memory ring of
+// Between warps w and w+1 (w < W-1) it goes through a shared-memory ring of
 // kCtaRing columns with flow control both ways (the producer waits for
 // room, the consumer for data), published in 32-column chunks.  The wrap
-// from warp 7 back to warp 0 goes through a full-width row in global memory
+// from warp W-1 back to warp 0 goes through a full-width row in global memory
 // (the same row the warp-per-pair fill uses), whose producer never waits:
 // that breaks the cycle of waits, so the pipeline cannot deadlock.  Warp 0
 // stages that row with cp.async as the warp-per-pair fill does, after
-// checking warp 7's progress counter.
+// checking warp W-1's progress counter.
 //
 // Every wait is bounded (FillArgs::spin_limit polls, kSpinLimit when it is
 // 0); a wait that runs out marks the pair TSQ_E_TIMEOUT and makes every
@@ -30,8 +33,6 @@
 namespace tsq {
 namespace fill {
 
-constexpr int kCtaWarps = 8;
-constexpr int kCtaThreads = kCtaWarps * 32;
 constexpr int kCtaRing = 256;               // inter-warp ring, columns (a multiple of kChunk)
 constexpr int kSpinLimit = 1 << 22;         // polls per wait before giving up
 
@@ -44,13 +45,24 @@ struct CtaTop<kOutIdent> {
   using T = int4;
 };
 
+// Warps per CTA for an output mode and alignment mode.
+__host__ __device__ constexpr int cta_warps(int out_mode, bool local) {
+  return (out_mode != kOutIdent && !local) ? 16 : 8;
+}
+
+// Control block after the rings: progress counters prod[W], cons[W], the
+// fail flag and two ints (task index, spare), then W reduction keys and W
+// counts.
+__host__ __device__ constexpr int cta_keys_offset(int W) { return (4 * (2 * W + 3) + 15) & ~15; }
+__host__ __device__ constexpr int cta_ctl_bytes(int W) { return (cta_keys_offset(W) + 12 * W + 15) & ~15; }
+
 // Shared-memory bytes of the CTA fill for an output mode.
-__host__ __device__ constexpr size_t cta_smem_bytes(int out_mode) {
-  return size_t(kMatBytes) + size_t(kLetters) * kCtaThreads * 8 +                     // matrix, profile
+__host__ __device__ constexpr size_t cta_smem_bytes(int out_mode, int W) {
+  return size_t(kMatBytes) + size_t(kLetters) * W * 32 * 8 +                           // matrix, profile
          size_t(kTopRing) * (out_mode == kOutIdent ? 16 : 8) + kRingPad +              // warp 0's staging ring
-         size_t(kCtaWarps) * (kCodeRing + kRingPad) +                                  // code rings
-         size_t(kCtaWarps - 1) * kCtaRing * (out_mode == kOutIdent ? 16 : 8) +         // inter-warp rings
-         256;                                                                          // counters
+         size_t(W) * (kCodeRing + kRingPad) +                                          // code rings
+         size_t(W - 1) * kCtaRing * (out_mode == kOutIdent ? 16 : 8) +                 // inter-warp rings
+         cta_ctl_bytes(W);                                                             // counters
 }
 
 // Warp-uniform poll of a shared counter until it reaches target.  False if
@@ -76,9 +88,10 @@ __device__ __forceinline__ bool cta_wait_geq(const volatile int *ctr, int target
   return false;
 }
 
-template <bool LOCAL, int OUT>
-__global__ void __launch_bounds__(kCtaThreads, 1) fill_cta_kernel(const FillArgs A) {
+template <bool LOCAL, int OUT, int W>
+__global__ void __launch_bounds__(W * 32, 1) fill_cta_kernel(const FillArgs A) {
   constexpr int G = 32, R = 8, P = G * R;
+  constexpr int kCtaWarps = W, kCtaThreads = W * 32;
   using Top = typename CtaTop<OUT>::T;
   extern __shared__ __align__(16) uint8_t smem[];
   int8_t *s_mat = reinterpret_cast<int8_t *>(smem);
@@ -88,14 +101,14 @@ __global__ void __launch_bounds__(kCtaThreads, 1) fill_cta_kernel(const FillArgs
   p += kTopRing * sizeof(Top) + kRingPad;
   uint8_t *code_rings = p;
   p += kCtaWarps * (kCodeRing + kRingPad);
-  Top *rings = reinterpret_cast<Top *>(p);  // ring w (w = 1..7) at rings + (w-1)*kCtaRing
+  Top *rings = reinterpret_cast<Top *>(p);  // ring w (w = 1..W-1) at rings + (w-1)*kCtaRing
   p += (kCtaWarps - 1) * kCtaRing * sizeof(Top);
   volatile int *prod = reinterpret_cast<volatile int *>(p);       // [kCtaWarps]
   volatile int *cons = prod + kCtaWarps;                           // [kCtaWarps]
   volatile int *fail = cons + kCtaWarps;
   int *s_misc = const_cast<int *>(fail) + 1;                       // task index, bad flag
-  int64_t *s_keys = reinterpret_cast<int64_t *>(p + 128);          // [kCtaWarps] local reductions
-  uint32_t *s_cnt = reinterpret_cast<uint32_t *>(p + 192);         // [kCtaWarps]
+  int64_t *s_keys = reinterpret_cast<int64_t *>(p + cta_keys_offset(W));           // [W] local reductions
+  uint32_t *s_cnt = reinterpret_cast<uint32_t *>(p + cta_keys_offset(W) + 8 * W);  // [W]
 
   for (int k = threadIdx.x; k < kLetters * kLetters; k += blockDim.x) s_mat[k] = A.matrix[k];
   __syncthreads();
@@ -197,7 +210,7 @@ __global__ void __launch_bounds__(kCtaThreads, 1) fill_cta_kernel(const FillArgs
       uint32_t outCH = 0, outCF = 0;
 
       // Where this band's top row comes from.  Warp 0: the global row (row
-      // 0, or warp 7's previous band, whose progress it checks first).
+      // 0, or warp W-1's previous band, whose progress it checks first).
       auto stage_global = [&](int chunk) {
         if (band > 0) cta_wait_geq(&prod[0], (i - 1) * n + min(kChunk * (chunk + 1), n), fail, spin);
         stage_chunk<G, Top>(chunk, t, n, grow, stage_ring, A.codes, boff, code_ring);
