@@ -234,7 +234,7 @@ class WorkerPool {
 template <class F>
 int parallel_for(int64_t n, F &&f) {
   WorkerPool &pool = WorkerPool::get();
-  const int slices = int(std::min<int64_t>({8, int64_t(pool.workers()) + 1, std::max<int64_t>(1, n / 4096)}));
+  const int slices = int(std::min<int64_t>({8, int64_t(pool.workers()) + 1, std::max<int64_t>(1, n / 1024)}));
   if (slices > 1) {
     const int64_t chunk = (n + slices - 1) / slices;
     const std::function<void(int)> task = [&](int i) {
@@ -281,20 +281,25 @@ int bit_width(uint64_t v) { return v == 0 ? 0 : 64 - __builtin_clzll(v); }
 
 }  // namespace
 
+void ShapeChooser::prepare() {
+  const int64_t target_warps = int64_t(sms) * 24;
+  g_occ = npairs > 0 ? pow2ceil((target_warps * 32 + npairs - 1) / npairs) : 32;
+  inv_half_lane_steps = avg_lane_steps > 0 ? 1.0 / (0.5 * avg_lane_steps) : 0.0;
+}
+
 Shape ShapeChooser::pick(int m, int n, int rows_per_lane) const {
   // Lanes per pair G: (1) enough groups to fill every SM about 24 warps
   // deep; (2) enough lanes that this pair's sweep -- about m*n / (G*R)
   // dependent steps -- stays under half the balanced per-lane work of the
   // batch, so a long pair does not become the tail; (3) no more lanes than
   // its rows can use.
-  const int64_t target_warps = int64_t(sms) * 24;
-  int g_occ = npairs > 0 ? pow2ceil((target_warps * 32 + npairs - 1) / npairs) : 32;
+  const int rshift = rows_per_lane == 16 ? 4 : 3;
   int g_lat = 1;
-  if (avg_lane_steps > 0) {
-    const double steps_at_g1 = double(m) * double(n) / rows_per_lane;
-    g_lat = pow2ceil(int64_t(steps_at_g1 / (0.5 * avg_lane_steps)) + 1);
+  if (inv_half_lane_steps > 0) {
+    const double steps_at_g1 = double(m) * double(n) * (1.0 / double(rows_per_lane));
+    g_lat = pow2ceil(int64_t(steps_at_g1 * inv_half_lane_steps) + 1);
   }
-  const int rows_cap = pow2ceil((m + rows_per_lane - 1) / rows_per_lane);
+  const int rows_cap = pow2ceil((m + rows_per_lane - 1) >> rshift);
   int G = std::max(g_occ, g_lat);
   if (force.shape) return force.sh;
   Shape sh{};
@@ -607,6 +612,7 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   }
   ch.use_table = b->autotune && tune_table_loaded();
   ch.force = b->tune_force;
+  ch.prepare();
   PlanScratch &ps = b->scratch;
   ps.lsel.resize(size_t(n));
   ps.gsel.resize(size_t(n));
@@ -618,9 +624,9 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   std::vector<int32_t> &rsel = ps.rsel;
   std::vector<SortRec> &recs = ps.recs;
   auto two_bands = [&](int64_t k) { return lsel[size_t(k)] == 1 || lsel[size_t(k)] == 2; };
-  auto bands = [&](int64_t k) {
+  auto bands = [&](int64_t k) {  // P = G * R (* 2): a power of two
     const int P = gsel[size_t(k)] * rsel[size_t(k)] * (two_bands(k) ? 2 : 1);
-    return (b->pairs_h[size_t(k)].a_len + P - 1) / P;
+    return (b->pairs_h[size_t(k)].a_len + P - 1) >> __builtin_ctz(unsigned(P));
   };
   auto steps = [&](int64_t k) {
     return b->pairs_h[size_t(k)].b_len + gsel[size_t(k)] * (two_bands(k) ? 2 : 1) - 1;

@@ -90,6 +90,13 @@ struct ShapeChooser {
   double avg_lane_steps = 0.0;
   bool use_table = false;
   TuneForce force;
+  // Set by prepare() from the fields above: the occupancy lane width and
+  // the reciprocal of half the balanced lane steps (the per-pair choice
+  // then takes no division).
+  int g_occ = 32;
+  double inv_half_lane_steps = 0.0;
+  void prepare();
+  // rows_per_lane: 8 or 16 (a power of two).
   Shape pick(int m, int n, int rows_per_lane) const;
 };
 
