@@ -355,6 +355,7 @@ int tsq_align_batch(const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *
       // object: residues, rows, results, strings).  Results land at the pairs' own
       // positions; a pair too large for any wave is TSQ_E_TOO_LARGE.
       if (cudaSetDevice(dev) != cudaSuccess) return TSQ_E_CUDA;
+      tsq::trim_engine_pool(dev);
       size_t free_b = 0, total_b = 0;
       if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return TSQ_E_CUDA;
       const double avail = double(free_b + e->planes.cap + e->aln.cap);

@@ -17,11 +17,59 @@
 #include <atomic>
 #include <condition_variable>
 #include <functional>
+#include <map>
 #include <mutex>
 #include <numeric>
 #include <thread>
 
 namespace tsq {
+
+namespace {
+// The engine's stream-ordered allocations come from a memory pool of its
+// own per device, which keeps freed memory mapped up to a release
+// threshold of 40 % of the device's memory (the default pool returns it at
+// every synchronisation).  Mapping is the slow part of a stream-ordered
+// allocation -- about 1 ms per GB on GB300 -- so a server whose traceback
+// ticks need gigabytes of planes pays it once, not per tick.
+cudaMemPool_t engine_pool(int dev) {
+  static std::mutex mu;
+  static std::map<int, cudaMemPool_t> pools;
+  std::lock_guard<std::mutex> g(mu);
+  const auto it = pools.find(dev);
+  if (it != pools.end()) return it->second;
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.handleTypes = cudaMemHandleTypeNone;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool = nullptr;
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemPoolCreate(&pool, &props) != cudaSuccess || cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+    cudaGetLastError();
+    if (pool) cudaMemPoolDestroy(pool);
+    pool = nullptr;
+  } else {
+    uint64_t keep = uint64_t(double(total_b) * 0.4);
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  pools[dev] = pool;  // (nullptr: the default pool is used)
+  return pool;
+}
+
+cudaMemPool_t engine_pool(cudaStream_t stream) {
+  int dev = 0;
+  if (cudaStreamGetDevice(stream, &dev) != cudaSuccess) {
+    cudaGetLastError();
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  }
+  return engine_pool(dev);
+}
+}  // namespace
+
+void trim_engine_pool(int device) {
+  cudaMemPool_t pool = engine_pool(device);
+  if (pool) cudaMemPoolTrimTo(pool, 0);
+}
 
 cudaError_t DevBuf::ensure(size_t bytes, cudaStream_t stream, size_t async_max) {
   if (bytes == 0) bytes = 16;
@@ -30,12 +78,19 @@ cudaError_t DevBuf::ensure(size_t bytes, cudaStream_t stream, size_t async_max) 
   release();
   // Stream-ordered allocation takes no device-wide synchronisation, so a
   // batch object that grows does not wait for kernels other streams run.
-  // It maps memory far more slowly, though (measured on GB300: 16 ms for
-  // 16 GB against 0.5 ms by cudaMalloc, 267 ms against 4.7 ms for 200 GB),
-  // so buffers from async_max up come from cudaMalloc, whose free waits for
-  // the device.
+  // Mapping new memory that way is slow, though (measured on GB300: 16 ms
+  // for 16 GB against 0.5 ms by cudaMalloc, 267 ms against 4.7 ms for
+  // 200 GB), so buffers from async_max up come from cudaMalloc, whose free
+  // waits for the device, and stream-ordered ones come from the engine's
+  // pool, which keeps freed memory mapped for the next allocation.
   const bool async = stream && want < async_max;
-  cudaError_t e = async ? cudaMallocAsync(&p, want, stream) : cudaMalloc(&p, want);
+  cudaError_t e = cudaSuccess;
+  if (async) {
+    cudaMemPool_t pool = engine_pool(stream);
+    e = pool ? cudaMallocFromPoolAsync(&p, want, pool, stream) : cudaMallocAsync(&p, want, stream);
+  } else {
+    e = cudaMalloc(&p, want);
+  }
   if (e != cudaSuccess) {
     p = nullptr;
     return e;

@@ -230,5 +230,8 @@ int batch_collect(tsq_batch *b, int64_t begin, int64_t count, tsq_result *out, c
 int64_t cost_order(const tsq_pair_desc *pairs, int64_t n, std::vector<uint8_t> &bin, tsq_pair_desc *out_pairs,
                    int32_t *out_index);
 int64_t batch_device_bytes(const tsq_batch *b);
+// Returns the memory the engine's stream-ordered pool keeps mapped on a
+// device but does not use (before a call sizes itself by the free memory).
+void trim_engine_pool(int device);
 int cuda_status(cudaError_t e);
 }  // namespace tsq
