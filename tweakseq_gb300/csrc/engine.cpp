@@ -25,6 +25,8 @@
 namespace tsq {
 
 namespace {
+void run_slices(int tasks, const std::function<void(int)> &task);
+
 // The engine's stream-ordered allocations come from a memory pool of its
 // own per device, which keeps freed memory mapped up to a release
 // threshold of 40 % of the device's memory (the default pool returns it at
@@ -65,6 +67,8 @@ cudaMemPool_t engine_pool(cudaStream_t stream) {
   return engine_pool(dev);
 }
 }  // namespace
+
+void run_tasks(int tasks, const std::function<void(int)> &task) { run_slices(tasks, task); }
 
 void trim_engine_pool(int device) {
   cudaMemPool_t pool = engine_pool(device);

@@ -3,6 +3,7 @@
 
 #include <cstdint>
 #include <string>
+#include <functional>
 #include <vector>
 
 #include "tsq_internal.h"
@@ -233,5 +234,8 @@ int64_t batch_device_bytes(const tsq_batch *b);
 // Returns the memory the engine's stream-ordered pool keeps mapped on a
 // device but does not use (before a call sizes itself by the free memory).
 void trim_engine_pool(int device);
+// Runs task(i) for i in [0, tasks) on the planner's host worker pool (in
+// turn on the calling thread when the pool is busy).
+void run_tasks(int tasks, const std::function<void(int)> &task);
 int cuda_status(cudaError_t e);
 }  // namespace tsq

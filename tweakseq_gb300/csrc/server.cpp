@@ -67,6 +67,9 @@ struct Slot {
   std::vector<int64_t> first;  // first pair of each request in the tick
   int64_t bytes = 0;           // reserved against the budget
   bool busy = false;
+  // The tick's residues: page-locked, so that their upload is a direct
+  // copy (a pageable vector when page-locked memory cannot be had).
+  std::unique_ptr<tsq::PinBuf> seqpin;
   std::vector<uint8_t> seqbuf;
   std::vector<tsq_pair_desc> pairbuf;
 };
@@ -138,19 +141,39 @@ struct tsq_server {
 int tsq_server::launch(Slot &s, std::vector<std::shared_ptr<Request>> &&reqs, int64_t bytes) {
   tsq::TraceRange tr("server tick launch");
   s.reqs = std::move(reqs);
-  s.first.clear();
-  s.seqbuf.clear();
-  s.pairbuf.clear();
-  for (const auto &r : s.reqs) {
-    const int64_t base = int64_t(s.seqbuf.size());
-    s.first.push_back(int64_t(s.pairbuf.size()));
-    s.seqbuf.insert(s.seqbuf.end(), r->seqs.begin(), r->seqs.end());
-    for (tsq_pair_desc d : r->pairs) {
+  // The tick's residues and pair table: each request's at its offsets,
+  // copied on the host worker pool (a tick can hold tens of megabytes).
+  const size_t nr = s.reqs.size();
+  std::vector<int64_t> seq_at(nr + 1, 0);
+  s.first.assign(nr + 1, 0);
+  for (size_t q = 0; q < nr; ++q) {
+    seq_at[q + 1] = seq_at[q] + int64_t(s.reqs[q]->seqs.size());
+    s.first[q + 1] = s.first[q] + int64_t(s.reqs[q]->pairs.size());
+  }
+  const int64_t seq_len = seq_at[nr];
+  uint8_t *seqs = nullptr;
+  if (!s.seqpin) s.seqpin.reset(new tsq::PinBuf());
+  if (s.seqpin->ensure(size_t(seq_len)) == cudaSuccess) {
+    seqs = s.seqpin->as<uint8_t>();
+  } else {
+    cudaGetLastError();
+    s.seqbuf.resize(size_t(seq_len));
+    seqs = s.seqbuf.data();
+  }
+  s.pairbuf.resize(size_t(s.first[nr]));
+  tsq::run_tasks(int(nr), [&](int q) {
+    const Request &r = *s.reqs[size_t(q)];
+    const int64_t base = seq_at[size_t(q)];
+    if (!r.seqs.empty()) std::memcpy(seqs + base, r.seqs.data(), r.seqs.size());
+    tsq_pair_desc *dst = s.pairbuf.data() + s.first[size_t(q)];
+    for (size_t k = 0; k < r.pairs.size(); ++k) {
+      tsq_pair_desc d = r.pairs[k];
       d.a_off += base;
       d.b_off += base;
-      s.pairbuf.push_back(d);
+      dst[k] = d;
     }
-  }
+  });
+  s.first.pop_back();
   if (!s.batch) {
     s.batch.reset(new tsq_batch());
     s.batch->async_max = SIZE_MAX;  // growth never waits for the other slots
@@ -164,7 +187,7 @@ int tsq_server::launch(Slot &s, std::vector<std::shared_ptr<Request>> &&reqs, in
   o.device = device;
   o.use_graph = 0;  // every tick is a different plan
   o.autotune = opts.autotune;
-  int rc = tsq::batch_plan(s.batch.get(), s.seqbuf.data(), int64_t(s.seqbuf.size()), s.pairbuf.data(),
+  int rc = tsq::batch_plan(s.batch.get(), seqs, seq_len, s.pairbuf.data(),
                            int64_t(s.pairbuf.size()), &p, &o, false);
   if (!rc) rc = tsq::batch_run_async(s.batch.get());
   if (!rc) rc = tsq::batch_fetch_async(s.batch.get());
@@ -175,12 +198,15 @@ int tsq_server::launch(Slot &s, std::vector<std::shared_ptr<Request>> &&reqs, in
 // Called with the lock held.
 void tsq_server::finish(Slot &s, int rc) {
   const auto now = Clock::now();
+  // Each request's results (and strings) are copied out of the tick's
+  // result blocks on the host worker pool.
+  tsq::run_tasks(int(s.reqs.size()), [&](int q) {
+    Request &r = *s.reqs[size_t(q)];
+    r.results.assign(r.pairs.size(), tsq_result{});
+    r.status = rc ? rc : tsq::batch_collect(s.batch.get(), s.first[size_t(q)], int64_t(r.pairs.size()), r.results.data());
+  });
   for (size_t q = 0; q < s.reqs.size(); ++q) {
     Request &r = *s.reqs[q];
-    r.results.assign(r.pairs.size(), tsq_result{});
-    int st = rc;
-    if (!rc) st = tsq::batch_collect(s.batch.get(), s.first[q], int64_t(r.pairs.size()), r.results.data());
-    r.status = st;
     r.state = Request::kDone;
     r.t_done = now;
     ++completed;
