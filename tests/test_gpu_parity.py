@@ -288,7 +288,9 @@ def test_int16_overflow_rerun_and_lane_choices(local):
     for lane in ("auto", "i16", "i32"):
         got = A.align_batch(ps, mode=mode, output="score", lane=lane)
         assert_same(got, want, score_fields(local), f"lane {lane}")
-    with A.Batch(ps, mode=mode, output="score", lane="auto") as b:
+    # (Lane auto sends the 3,100 and 3,500-residue pairs to the CTA fill in
+    # int32; lane i16 keeps them on the checked int16x2 kernel.)
+    with A.Batch(ps, mode=mode, output="score", lane="i16") as b:
         b.run()
         assert_same(b.results(), want, score_fields(local), "batch")
         assert b.stats()["rerun_pairs"] >= 3  # 2979, 3100 and 3500 overflow (2978 is flagged too)
@@ -329,7 +331,7 @@ def test_int16_traceback_and_identity_fills_at_the_overflow_edge(output, local):
         assert_same(got, want, fields, f"{output} lane {lane}")
         if sa is not None:
             assert got.aln_a == sa and got.aln_b == sb, f"strings, lane {lane}"
-    with A.Batch(ps, mode=mode, output=output, lane="auto") as b:
+    with A.Batch(ps, mode=mode, output=output, lane="i16") as b:
         b.run()
         assert_same(b.results(), want, fields, "batch")
         assert b.stats()["rerun_pairs"] >= 2  # 2979 and 3100 overflow
@@ -391,8 +393,8 @@ def test_mixed_lane_types_one_batch():
 
 @pytest.mark.parametrize("local", [False, True])
 def test_long_pairs_on_the_cta_fill_all_outputs(local):
-    """Pairs long enough for the CTA fill (bands striped over 8 warps):
-    79, 12 and 3 bands (fewer bands than warps), long rows and long
+    """Pairs long enough for the CTA fill (bands striped over the warps of
+    a CTA): 79, 12 and 3 bands (fewer bands than warps), long rows and long
     columns, score / identity / alignment, against the oracle."""
     rng = np.random.default_rng(17 + local)
     seqs, pairs = [], []
@@ -404,14 +406,17 @@ def test_long_pairs_on_the_cta_fill_all_outputs(local):
         seqs += [a.tobytes(), b.tobytes()]
         pairs.append((len(seqs) - 2, len(seqs) - 1))
     ps = W._pairset_from_lists(seqs, pairs, matrix=W.DNA, gap_open=5, gap_extend=2)
-    got = gpu_batch(ps, local, "score")
-    assert_same(got, oracle_batch(ps, local, O.MODE_SCORE), score_fields(local), "cta score")
-    got = gpu_batch(ps, local, "identity")
-    assert_same(got, oracle_batch(ps, local, O.MODE_IDENT), ident_fields(local), "cta identity")
-    got = gpu_batch(ps, local, "alignment")
     want, sa, sb = oracle_batch(ps, local, O.MODE_ALIGN, strings=True)
-    assert_same(got, want, FIELDS, "cta alignment")
-    assert got.aln_a == sa and got.aln_b == sb
+    # lane auto: the 20 kb pairs (past the int16 range) on the CTA fill,
+    # the others on int16x2 lanes; lane i32: all four on the CTA fill.
+    for lane in ("auto", "i32"):
+        got = gpu_batch(ps, local, "score", lane=lane)
+        assert_same(got, oracle_batch(ps, local, O.MODE_SCORE), score_fields(local), f"cta score {lane}")
+        got = gpu_batch(ps, local, "identity", lane=lane)
+        assert_same(got, oracle_batch(ps, local, O.MODE_IDENT), ident_fields(local), f"cta identity {lane}")
+        got = gpu_batch(ps, local, "alignment", lane=lane)
+        assert_same(got, want, FIELDS, f"cta alignment {lane}")
+        assert got.aln_a == sa and got.aln_b == sb
     # The plain form of a long pair takes the same path.
     a, b = ps.pair(2)
     r = A.align_pair(a, b, matrix="dna", gap_open=5, gap_extend=2, mode="local" if local else "global")
