@@ -563,6 +563,30 @@ def configs_leg(c3_pairs=12):
     t0 = time.perf_counter()
     A.align_batch(ps, output="alignment")
     e2e_s = time.perf_counter() - t0
+    # The same call at the C ABI, as a C or C++ caller makes it: pinned
+    # residues, host pair table and tsq_result array, the strings freed
+    # after each call; the median of 5 calls after a warm-up.
+    import torch
+
+    from tweakseq_gb300 import _native as N
+    pinned = torch.empty(len(ps.seqs), dtype=torch.uint8, pin_memory=True)
+    pinned.numpy()[:] = ps.seqs
+    tab = A.pair_table(ps.a_off, ps.a_len, ps.b_off, ps.b_len)
+    raw = np.zeros(len(tab), dtype=N.RESULT_DTYPE)
+    params, keep_params = N.make_params(output="alignment")
+    opts = A._opts()
+    L = N.lib()
+    c_times = []
+    for it in range(6):
+        t0 = time.perf_counter()
+        rc = L.tsq_align_batch(pinned.data_ptr(), len(ps.seqs), tab.ctypes.data, len(tab), ctypes.byref(params),
+                               ctypes.byref(opts), raw.ctypes.data)
+        c_s = time.perf_counter() - t0
+        N.check(rc, "tsq_align_batch")
+        L.tsq_results_free(raw.ctypes.data, len(raw))
+        if it > 0:
+            c_times.append(c_s)
+    c_abi_s = float(np.median(c_times))
     t0 = time.perf_counter()
     for k in range(len(ps)):
         a, bb = ps.pair(k)
@@ -575,6 +599,9 @@ def configs_leg(c3_pairs=12):
     out["all_vs_all_64_proteins"] = {
         "pairs": len(ps), "cells": ps.cells, "output": "alignment (global, BLOSUM62 11/1)",
         "batched_gcups": ps.cells / (float(np.median(ms)) * 1e-3) / 1e9, "e2e_gcups": ps.cells / e2e_s / 1e9,
+        "e2e_c_abi_gcups": ps.cells / c_abi_s / 1e9, "e2e_c_abi_ms": c_abi_s * 1e3,
+        "e2e_note": "e2e_gcups: through the Python API (Python string objects included); e2e_c_abi: "
+                    "tsq_align_batch with host buffers, strings freed per call",
         "plain_gcups": ps.cells / plain_s / 1e9, "mismatches_vs_oracle": mism}
     # Full traceback on the headline's 100,000 uneven pairs: the int16x2
     # traceback fill (planes in HBM) and the walker, device-resident, next
