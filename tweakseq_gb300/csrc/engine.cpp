@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
 #include <functional>
 #include <map>
@@ -233,7 +234,7 @@ class WorkerPool {
       tasks_ = tasks;
       next_.store(0);
       left_ = tasks;
-      ++gen_;
+      gen_.fetch_add(1);
     }
     cv_.notify_all();
     work();
@@ -253,6 +254,7 @@ class WorkerPool {
     {
       std::lock_guard<std::mutex> g(mu_);
       stop_ = true;
+      stop_flag_.store(true);
     }
     cv_.notify_all();
     for (std::thread &t : threads_) t.join();
@@ -269,11 +271,18 @@ class WorkerPool {
   void loop() {
     uint64_t seen = 0;
     for (;;) {
+      // A plan runs several passes in a row: after a job, poll for the next
+      // one for about 50 microseconds before sleeping (waking a sleeping
+      // worker costs tens of microseconds per pass).
+      const auto t0 = std::chrono::steady_clock::now();
+      while (gen_.load(std::memory_order_acquire) == seen && !stop_flag_.load(std::memory_order_relaxed) &&
+             std::chrono::steady_clock::now() - t0 < std::chrono::microseconds(50)) {
+      }
       {
         std::unique_lock<std::mutex> g(mu_);
-        cv_.wait(g, [&] { return stop_ || gen_ != seen; });
+        cv_.wait(g, [&] { return stop_ || gen_.load() != seen; });
         if (stop_) return;
-        seen = gen_;
+        seen = gen_.load();
       }
       work();
     }
@@ -284,8 +293,9 @@ class WorkerPool {
   const std::function<void(int)> *task_ = nullptr;
   int tasks_ = 0, left_ = 0;
   std::atomic<int> next_{0};
-  uint64_t gen_ = 0;
+  std::atomic<uint64_t> gen_{0};
   bool stop_ = false;
+  std::atomic<bool> stop_flag_{false};
 };
 
 // Runs f(begin, end, slot) over [0, n) in up to 8 slices (slot = slice
