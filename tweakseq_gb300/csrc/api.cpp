@@ -355,16 +355,6 @@ int tsq_align_batch(const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *
       // object: residues, rows, results, strings).  Results land at the pairs' own
       // positions; a pair too large for any wave is TSQ_E_TOO_LARGE.
       if (cudaSetDevice(dev) != cudaSuccess) return TSQ_E_CUDA;
-      tsq::trim_engine_pool(dev);
-      size_t free_b = 0, total_b = 0;
-      if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return TSQ_E_CUDA;
-      const double avail = double(free_b + e->planes.cap + e->aln.cap);
-      int64_t budget = std::max(int64_t(0.85 * avail) - (int64_t(2) << 30), int64_t(0.5 * avail));
-      // TSQ_WAVE_BUDGET_BYTES lowers the budget (tests use it to force waves).
-      if (const char *env = std::getenv("TSQ_WAVE_BUDGET_BYTES")) {
-        const long long v = std::atoll(env);
-        if (v > 0) budget = std::min<int64_t>(budget, v);
-      }
       std::vector<int64_t> bytes(static_cast<size_t>(n));
       int64_t total = 0;
       for (int64_t k = 0; k < n; ++k) {
@@ -372,6 +362,27 @@ int tsq_align_batch(const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *
         bytes[size_t(k)] = (std::max<int64_t>(d.a_len, 0) + 255) * (std::max<int64_t>(d.b_len, 0) + 31) / 2 +
                            2 * (int64_t(std::max(d.a_len, 0)) + std::max(d.b_len, 0)) + 512;
         total += bytes[size_t(k)];
+      }
+      auto wave_budget = [&](int64_t *budget) {
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return false;
+        const double avail = double(free_b + e->planes.cap + e->aln.cap);
+        *budget = std::max(int64_t(0.85 * avail) - (int64_t(2) << 30), int64_t(0.5 * avail));
+        // TSQ_WAVE_BUDGET_BYTES lowers the budget (tests use it to force waves).
+        if (const char *env = std::getenv("TSQ_WAVE_BUDGET_BYTES")) {
+          const long long v = std::atoll(env);
+          if (v > 0) *budget = std::min<int64_t>(*budget, v);
+        }
+        return true;
+      };
+      int64_t budget = 0;
+      if (!wave_budget(&budget)) return TSQ_E_CUDA;
+      if (total > budget) {
+        // Memory the engine's pool keeps mapped but does not use goes back
+        // first (only when the batch would not fit: unmapping costs about as
+        // much as mapping).
+        tsq::trim_engine_pool(dev);
+        if (!wave_budget(&budget)) return TSQ_E_CUDA;
       }
       if (total > budget) return align_in_waves(e, seqs, seqs_len, pairs, n, p, opts, out, bytes, budget);
     }
