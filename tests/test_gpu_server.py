@@ -175,6 +175,25 @@ def _resident_requests(seed):
             ps, kw = _protein_pairs(rng, int(rng.integers(5, 60)), 100, 1800), dict(output="identity")
         reqs.append((ps, kw))
     reqs.append((_protein_pairs(rng, 3, 2100, 2300), dict(output="score")))  # too long for the loop
+    # A custom matrix scoring 25 per identical letter: in the loop, pairs
+    # whose score bound passes 32767 run the checked int16x2 fill, and the
+    # 1,400-residue W:W pair (35,000) comes near 32767 and re-runs in int32;
+    # the 1,300-residue one (32,500) stays in int16x2.
+    mat = np.full((26, 26), -2, dtype=np.int8)
+    np.fill_diagonal(mat, 25)
+    custom = (mat, np.ones(26, dtype=np.uint8))
+    wseqs = [b"W" * 1400, b"W" * 1400, b"W" * 1300, b"W" * 1300]
+    wpairs = [(0, 1), (2, 3)]
+    for k in range(6):
+        a = W.random_protein(rng, int(rng.integers(900, 2000))).tobytes()
+        wseqs += [a, a[::-1]]
+        wpairs.append((len(wseqs) - 2, len(wseqs) - 1))
+    cps = W._pairset_from_lists(wseqs, wpairs)
+    reqs.append((cps, dict(output="score", custom=custom)))
+    reqs.append((cps, dict(output="identity", custom=custom)))
+    # Lane choices reach the loop: int32 only, and checked int16x2 for all.
+    reqs.append((_protein_pairs(rng, 20, 50, 900), dict(output="score", lane="i32")))
+    reqs.append((_protein_pairs(rng, 20, 50, 900), dict(output="identity", lane="i16")))
     bad = W._pairset_from_lists([b"ACDEFGHIK", b"ACDEFGHIK", b"AC*EF"], [(0, 1), (0, 2)])
     reqs.append((bad, dict(output="score")))
     return reqs

@@ -206,11 +206,14 @@ __device__ __forceinline__ bool range_has_bad(const uint8_t *p, int len, int t, 
 }
 
 // The lane width G is a run-time value: one code path serves every width,
-// which keeps the kernel small enough for the instruction cache.
+// which keeps the kernel small enough for the instruction cache.  With
+// warp_rings set (one 32-lane group per warp), the group's rings sit there
+// -- the top ring, then the code ring -- instead of in the block's ring
+// area.
 template <bool LOCAL, bool CHECK, int OUT>
 __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t *s_mat, uint2 *s_prof,
                                                  uint32_t *s_match, uint8_t *s_rings, int begin, int count,
-                                                 int warp_id, int G, int lg) {
+                                                 int warp_id, int G, int lg, uint8_t *warp_rings = nullptr) {
   static_assert(!(OUT == kOutIdent && LOCAL), "the int16x2 identity fill is global only");
   using Top = typename Top16<OUT>::T;
   constexpr int R = 8;
@@ -234,8 +237,9 @@ __device__ __forceinline__ void fill16_warp_task(const FillArgs &A, const int8_t
   Top *top = reinterpret_cast<Top *>(A.bnd) + ((int64_t)warp_id * 8 + gw) * A.bnd_cols;
   const int gslot = (threadIdx.x >> 5) * 8 + gw;
   constexpr int kTopStride = kTopRing * int(sizeof(Top)) + kRingPad;  // bytes
-  Top *top_ring = reinterpret_cast<Top *>(s_rings + gslot * kTopStride);
-  uint8_t *code_ring = s_rings + kSlots16 * kTopStride + gslot * (kCodeRing16 + kRingPad);
+  Top *top_ring = reinterpret_cast<Top *>(warp_rings ? warp_rings : s_rings + gslot * kTopStride);
+  uint8_t *code_ring = warp_rings ? warp_rings + kTopStride
+                                  : s_rings + kSlots16 * kTopStride + gslot * (kCodeRing16 + kRingPad);
   const uint2 *profA = s_prof + threadIdx.x;                // + (2c) * kThreads16
   const uint2 *profB = s_prof + kThreads16 + threadIdx.x;   // + (2c) * kThreads16
   const int src_lane = (lane & ~(G - 1)) | ((t + G - 1) & (G - 1));  // rotate within the group
@@ -789,6 +793,10 @@ __host__ __device__ constexpr size_t smem16_match_bytes(int out_mode, int nclass
 }
 __host__ __device__ constexpr size_t smem16_top_stride(int out_mode) {
   return size_t(kTopRing) * (out_mode == kOutIdent ? 16 : 4) + kRingPad;
+}
+// Bytes of one group's private rings (the warp_rings layout).
+__host__ __device__ constexpr size_t warp_rings16_bytes(int out_mode) {
+  return smem16_top_stride(out_mode) + kCodeRing16 + kRingPad;
 }
 
 template <bool LOCAL, bool CHECK, int OUT>

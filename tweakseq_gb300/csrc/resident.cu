@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "fill_i16.cuh"
 #include "fill_i32.cuh"
 #include "trace.h"
 
@@ -13,14 +14,25 @@ namespace {
 
 constexpr int kBndCols = ((kMaxLen + 31) / 32 + 1) * 32;  // one staged chunk past the longest row
 constexpr size_t kMatSlot = 704;                           // 26 x 26 int8, per warp
+constexpr size_t kMatSlot16 = fill::kMatBytes16;           // class matrix of the int16x2 fill, per warp
 constexpr int kWarps = fill::kThreads / 32;
+static_assert(fill::kThreads == fill::kThreads16, "both fills index their profiles by the same thread");
 
-// Each warp's private rings: one 32-lane group, top-row entries of up to 16
-// bytes (identity mode), then the code ring.
-constexpr size_t kWarpRings = size_t(fill::kTopRing) * 16 + fill::kRingPad + fill::kCodeRing + fill::kRingPad;
+// Each warp's private rings: one 32-lane group, as large as the int32
+// fill's (top-row entries of up to 16 bytes, 128-byte code ring) or the
+// int16x2 fill's (up to 16-byte entries, 256-byte code ring) need.
+constexpr size_t kWarpRings32 = size_t(fill::kTopRing) * 16 + fill::kRingPad + fill::kCodeRing + fill::kRingPad;
+constexpr size_t kWarpRings =
+    kWarpRings32 > fill::warp_rings16_bytes(kOutIdent) ? kWarpRings32 : fill::warp_rings16_bytes(kOutIdent);
+
+// Per-thread profile area: the int16x2 fill's (two 8-row words per class,
+// 26 classes at most) holds the int32 fill's (one word per letter); a
+// thread uses one of them at a time.  Then the identity match table.
+constexpr size_t kProfBytes = fill::smem16_prof_bytes(kLetters);
+constexpr size_t kMatchBytes = fill::smem16_match_bytes(kOutIdent, kLetters);
 
 __host__ __device__ constexpr size_t smem_bytes() {
-  return size_t(kWarps) * kMatSlot + size_t(kLetters) * fill::kThreads * 8 + size_t(kWarps) * kWarpRings;
+  return size_t(kWarps) * (kMatSlot + kMatSlot16) + kProfBytes + kMatchBytes + size_t(kWarps) * kWarpRings;
 }
 
 __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p) {
@@ -36,17 +48,28 @@ __device__ __forceinline__ void run_pair(const FillArgs &a, const int8_t *s_mat,
   fill::fill_warp_task<32, 8, LOCAL, OUT>(a, s_mat, s_prof, s_rings, 0, 1, 0, my_rings);
 }
 
+// Runs one pair with the int16x2 fill of fill_i16.cuh on a 32-lane group.
+template <bool LOCAL, bool CHECK, int OUT>
+__device__ __forceinline__ void run_pair16(const FillArgs &a, const int8_t *s_mat16, uint2 *s_prof, uint32_t *s_match,
+                                           uint8_t *my_rings) {
+  fill::fill16_warp_task<LOCAL, CHECK, OUT>(a, s_mat16, s_prof, s_match, nullptr, 0, 1, 0, 32, 5, my_rings);
+}
+
 __global__ void __launch_bounds__(fill::kThreads, 1)
     resident_kernel(const ReqDesc *reqs, const Task *ring, Ctl *ctl, HostBlock *host, int32_t *bnd, int32_t idle_polls) {
   extern __shared__ __align__(16) uint8_t smem[];
+  __shared__ int32_t s_pair[kWarps];  // the decoded pair index of each warp's task
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int8_t *s_mat = reinterpret_cast<int8_t *>(smem + size_t(w) * kMatSlot);
-  uint2 *s_prof = reinterpret_cast<uint2 *>(smem + size_t(kWarps) * kMatSlot);
-  uint8_t *s_rings = smem + size_t(kWarps) * kMatSlot + size_t(kLetters) * fill::kThreads * 8;
+  int8_t *s_mat16 = reinterpret_cast<int8_t *>(smem + size_t(kWarps) * kMatSlot + size_t(w) * kMatSlot16);
+  uint8_t *p = smem + size_t(kWarps) * (kMatSlot + kMatSlot16);
+  uint2 *s_prof = reinterpret_cast<uint2 *>(p);
+  uint32_t *s_match = reinterpret_cast<uint32_t *>(p + kProfBytes);
+  uint8_t *s_rings = p + kProfBytes + kMatchBytes;
   uint8_t *my_rings = s_rings + size_t(w) * kWarpRings;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int32_t *my_bnd = bnd + size_t(warp) * kBndCols * 4;  // one row of int4 entries
-  const int8_t *cached = nullptr;
+  uint64_t cached = 0, cached16 = 0;  // publication whose matrices this warp holds (0: none)
   int idle = 0;
   bool stopped = false;
   for (;;) {
@@ -77,38 +100,94 @@ __global__ void __launch_bounds__(fill::kThreads, 1)
     __threadfence();  // the task and its request were published before the tail
     const Task task = ring[idx & (kRingCap - 1)];
     const ReqDesc rq = reqs[task.req];
-    if (rq.matrix != cached) {
+    const int32_t pair = task.pair & 0xFFFFFF, lane_type = task.pair >> 24;
+    const bool packed = lane_type != kLaneI32;
+    if (lane == 0) s_pair[w] = pair;
+    if (rq.uid != cached) {
       for (int k = lane; k < kLetters * kLetters; k += 32) s_mat[k] = rq.matrix[k];
-      __syncwarp();
-      cached = rq.matrix;
+      cached = rq.uid;
     }
-    // The pair's letter codes, written by this warp (another warp coding a
-    // shared sequence writes the same bytes); the fill reads them below.
+    if (packed && rq.uid != cached16) {
+      // Class scores, one 32-byte row per class, then a zero row for the
+      // padding rows (index nclasses).
+      for (int k = lane; k < int(kMatSlot16); k += 32) {
+        const int x = k / fill::kMatRow16, c = k % fill::kMatRow16;
+        s_mat16[k] = (x < rq.nclasses && c < rq.nclasses) ? rq.cmatrix[x * rq.nclasses + c] : int8_t(0);
+      }
+      cached16 = rq.uid;
+    }
+    // The pair's letter codes (and, for the packed fill, class codes),
+    // written by this warp (another warp coding a shared sequence writes the
+    // same bytes); the fill reads them below.  The packed fill's staging
+    // reads class codes up to 64 bytes past a sequence and uses them as
+    // profile indices unchecked: those are written too, from the residues
+    // and the buffer's padding (class 0 for any byte outside the scheme).
     {
-      const PairDev pd = rq.pairs[task.pair];
+      const PairDev pd = rq.pairs[pair];
       for (int k = lane; k < pd.a_len; k += 32) rq.codes[pd.a_off + k] = rq.lut[rq.seqs[pd.a_off + k]];
       for (int k = lane; k < pd.b_len; k += 32) rq.codes[pd.b_off + k] = rq.lut[rq.seqs[pd.b_off + k]];
+      if (packed) {
+        const int64_t lim = rq.seqs_len + 128;
+        for (int64_t k = pd.a_off + lane; k < min(pd.a_off + pd.a_len + 64, lim); k += 32)
+          rq.ccodes[k] = rq.clut[rq.seqs[k]];
+        for (int64_t k = pd.b_off + lane; k < min(pd.b_off + pd.b_len + 64, lim); k += 32)
+          rq.ccodes[k] = rq.clut[rq.seqs[k]];
+        // The code ring may hold another fill's letter codes (up to 0xFF);
+        // the packed step reads ring bytes as class indices unchecked.
+        uint8_t *code_ring = my_rings + fill::smem16_top_stride(rq.out == kOutIdent ? kOutIdent : kOutScore);
+        for (int k = lane; k < fill::kCodeRing16 + fill::kRingPad; k += 32) code_ring[k] = 0;
+      }
       __syncwarp();
     }
     FillArgs a{};
     a.codes = rq.codes;
     a.pairs = rq.pairs;
-    a.tasks = &ring[idx & (kRingCap - 1)].pair;
+    a.tasks = &s_pair[w];
     a.gap_open = rq.gap_open;
     a.gap_extend = rq.gap_extend;
     a.res = rq.res;
     a.bnd = my_bnd;
     a.bnd_cols = kBndCols;
-    if (rq.out == kOutIdent) {
-      if (rq.local)
-        run_pair<true, kOutIdent>(a, s_mat, s_prof, s_rings, my_rings);
-      else
-        run_pair<false, kOutIdent>(a, s_mat, s_prof, s_rings, my_rings);
-    } else {
-      if (rq.local)
-        run_pair<true, kOutScore>(a, s_mat, s_prof, s_rings, my_rings);
-      else
-        run_pair<false, kOutScore>(a, s_mat, s_prof, s_rings, my_rings);
+    bool rerun = !packed;
+    if (packed) {
+      a.one = 1u;
+      a.ccodes = rq.ccodes;
+      a.nclasses = rq.nclasses;
+      a.max_score = rq.max_score;
+      a.overflow = rq.overflow;
+      const bool check = lane_type == kLaneI16Checked;
+      if (rq.out == kOutIdent) {
+        if (check)
+          run_pair16<false, true, kOutIdent>(a, s_mat16, s_prof, s_match, my_rings);
+        else
+          run_pair16<false, false, kOutIdent>(a, s_mat16, s_prof, s_match, my_rings);
+      } else if (rq.local) {
+        if (check)
+          run_pair16<true, true, kOutScore>(a, s_mat16, s_prof, s_match, my_rings);
+        else
+          run_pair16<true, false, kOutScore>(a, s_mat16, s_prof, s_match, my_rings);
+      } else {
+        if (check)
+          run_pair16<false, true, kOutScore>(a, s_mat16, s_prof, s_match, my_rings);
+        else
+          run_pair16<false, false, kOutScore>(a, s_mat16, s_prof, s_match, my_rings);
+      }
+      __syncwarp();
+      // A checked pair that came near 32767 runs again in int32.
+      if (check) rerun = *reinterpret_cast<volatile int32_t *>(&rq.overflow[pair]) != 0;
+    }
+    if (rerun) {
+      if (rq.out == kOutIdent) {
+        if (rq.local)
+          run_pair<true, kOutIdent>(a, s_mat, s_prof, s_rings, my_rings);
+        else
+          run_pair<false, kOutIdent>(a, s_mat, s_prof, s_rings, my_rings);
+      } else {
+        if (rq.local)
+          run_pair<true, kOutScore>(a, s_mat, s_prof, s_rings, my_rings);
+        else
+          run_pair<false, kOutScore>(a, s_mat, s_prof, s_rings, my_rings);
+      }
     }
     __syncwarp();
     if (lane == 0) {
@@ -131,15 +210,21 @@ int64_t align256(int64_t x) { return (x + 255) & ~int64_t(255); }
 
 // Where a request's buffers sit in its arena range.  What the host sends
 // comes first, in one block -- the residues (with 128 bytes of padding),
-// the pair table, the 26 x 26 matrix (a 1 KiB slot) and the letter table
-// -- then what the kernel writes: the letter codes and the results.
+// the pair table, the 26 x 26 matrix (a 1 KiB slot), the letter table, the
+// class scores (a 1 KiB slot) and the class table -- then what the kernel
+// writes: the letter codes, the class codes, the results and the
+// overflow flags of the checked int16x2 pairs.
 struct Layout {
   uint8_t *seqs;
   PairDev *pairs;
   int8_t *mat;
   uint8_t *lut;
+  int8_t *cmat;
+  uint8_t *clut;
   uint8_t *codes;
+  uint8_t *ccodes;
   ResultDev *res;
+  int32_t *overflow;
   int64_t host_bytes;  // the block the host sends
 };
 
@@ -149,8 +234,12 @@ Layout layout(uint8_t *arena, const Range &range, int64_t len, int64_t n) {
   l.pairs = reinterpret_cast<PairDev *>(l.seqs + align256(len + 128));
   l.mat = reinterpret_cast<int8_t *>(reinterpret_cast<uint8_t *>(l.pairs) + align256(24 * n));
   l.lut = reinterpret_cast<uint8_t *>(l.mat) + 1024;
-  l.codes = l.lut + 256;
-  l.res = reinterpret_cast<ResultDev *>(l.codes + align256(len + 128));
+  l.cmat = reinterpret_cast<int8_t *>(l.lut + 256);
+  l.clut = reinterpret_cast<uint8_t *>(l.cmat) + 1024;
+  l.codes = l.clut + 256;
+  l.ccodes = l.codes + align256(len + 128);
+  l.res = reinterpret_cast<ResultDev *>(l.ccodes + align256(len + 128));
+  l.overflow = reinterpret_cast<int32_t *>(reinterpret_cast<uint8_t *>(l.res) + align256(32 * n));
   l.host_bytes = l.codes - l.seqs;
   return l;
 }
@@ -158,13 +247,13 @@ Layout layout(uint8_t *arena, const Range &range, int64_t len, int64_t n) {
 }  // namespace
 
 int64_t arena_need(int64_t seqs_len, int64_t n) {
-  return 2 * align256(seqs_len + 128) + align256(24 * n) + align256(32 * n) + 1024 + 256;
+  return 3 * align256(seqs_len + 128) + align256(24 * n) + align256(32 * n) + align256(4 * n) + 2 * (1024 + 256);
 }
 
 // Bytes of the page-locked block a request is staged in: the arena block
 // the host sends, then the request descriptor and the tasks.
 int64_t stage_bytes(int64_t seqs_len, int64_t n) {
-  return align256(seqs_len + 128) + align256(24 * n) + 1024 + 256 + 256 + 8 * n;
+  return align256(seqs_len + 128) + align256(24 * n) + 2 * (1024 + 256) + 256 + 8 * n;
 }
 
 Loop::~Loop() { shutdown(); }
@@ -273,16 +362,43 @@ int Loop::publish(int32_t slot, const Range &range, const std::vector<uint8_t> &
   const int64_t off_pairs = reinterpret_cast<uint8_t *>(l.pairs) - l.seqs;
   const int64_t off_mat = reinterpret_cast<uint8_t *>(l.mat) - l.seqs;
   const int64_t off_lut = l.lut - l.seqs;
+  const int64_t off_cmat = reinterpret_cast<uint8_t *>(l.cmat) - l.seqs;
+  const int64_t off_clut = l.clut - l.seqs;
   if (len > 0) std::memcpy(h, seqs.data(), size_t(len));
+  // The 128 bytes of padding past the residues: the packed fill's class
+  // codes are written from them (any byte outside the scheme is class 0).
+  std::memset(h + len, 0, 128);
   std::memcpy(h + off_pairs, pairs.data(), size_t(24 * n));
   std::memcpy(h + off_mat, sc.score, sizeof(sc.score));
   build_lut(sc, h + off_lut);
+  std::memcpy(h + off_cmat, sc.cscore, size_t(sc.nclasses) * size_t(sc.nclasses));
+  build_class_lut(sc, h + off_clut);
   static_assert(sizeof(PairDev) == sizeof(tsq_pair_desc), "pair layouts must match");
+  const int out_mode = q.output == TSQ_OUT_IDENTITY ? int32_t(kOutIdent) : int32_t(kOutScore);
   ReqDesc *desc = reinterpret_cast<ReqDesc *>(h + l.host_bytes);
-  *desc = ReqDesc{l.seqs, l.codes, l.lut, l.pairs, l.res, l.mat, q.gap_open, q.gap_extend,
-                  q.mode == TSQ_LOCAL ? 1 : 0, q.output == TSQ_OUT_IDENTITY ? int32_t(kOutIdent) : int32_t(kOutScore)};
+  *desc = ReqDesc{l.seqs,     l.codes,       l.lut,      l.pairs,       l.res,        l.mat,
+                  q.gap_open, q.gap_extend,  q.mode == TSQ_LOCAL ? 1 : 0, out_mode,    l.ccodes,
+                  l.clut,     l.cmat,        l.overflow, len,           sc.nclasses,  sc.max_score,
+                  ++published_};
+  // Lane type per pair, by the batch planner's range rules: int16x2 where
+  // every value provably fits, checked int16x2 where only the lower bound
+  // is proven (or lane TSQ_LANE_I16 asks for it), int32 otherwise (and for
+  // local identity, which has no int16x2 fill).
+  const bool try16 = q.lane != TSQ_LANE_I32 && !(out_mode == kOutIdent && q.mode == TSQ_LOCAL);
+  const int64_t go = q.gap_open, ge = q.gap_extend;
+  const int64_t smax = std::max<int32_t>(sc.max_score, 0), sneg = std::max<int64_t>(0, -int64_t(sc.min_score));
   Task *tasks = reinterpret_cast<Task *>(h + l.host_bytes + 256);
-  for (int64_t k = 0; k < n; ++k) tasks[k] = Task{slot, int32_t(k)};
+  for (int64_t k = 0; k < n; ++k) {
+    const tsq_pair_desc &d = pairs[size_t(k)];
+    int32_t lt = kLaneI32;
+    if (try16) {
+      const int64_t lowest = 3 * go + (int64_t(d.a_len) + 512 + d.b_len + 1) * ge + go + ge + 128 + sneg;
+      const bool lower_ok = lowest + go + ge < 31000 && ge <= 700;
+      const bool upper_ok = smax * std::min(d.a_len, d.b_len) + smax < 32767;
+      if (lower_ok) lt = (upper_ok && q.lane == TSQ_LANE_AUTO) ? kLaneI16 : kLaneI16Checked;
+    }
+    tasks[k] = Task{slot, int32_t(k) | (lt << 24)};
+  }
   host_->done[slot] = 0;
   cudaStream_t st = ustream_;
   if (cudaMemcpyAsync(l.seqs, h, size_t(l.host_bytes), cudaMemcpyHostToDevice, st) != cudaSuccess ||

@@ -18,6 +18,12 @@
 // memory; the host relaunches it when work arrives.  A stop flag in mapped
 // memory ends it at once.
 //
+// Each pair runs in packed int16x2 (the fill of fill_i16.cuh on 32 lanes,
+// class codes written by the kernel beside the letter codes) when the
+// batch planner's range rules allow it -- checked pairs that come near
+// 32767 re-run in int32 in the same warp -- and in int32 otherwise; the
+// lane type travels in the task.
+//
 // Scope: score and identity requests (global or local, any matrix) whose
 // pairs are at most kMaxLen residues long; alignment requests and longer
 // pairs are served by ticks.
@@ -49,10 +55,25 @@ struct ReqDesc {  // one request, in device memory
   const int8_t *matrix;  // 26 x 26
   int32_t gap_open, gap_extend;
   int32_t local, out;
+  // int16x2 lanes: class codes (written by the kernel), byte -> class,
+  // the nclasses x nclasses class scores, per-pair overflow flags.
+  uint8_t *ccodes;
+  const uint8_t *clut;
+  const int8_t *cmatrix;
+  int32_t *overflow;
+  int64_t seqs_len;
+  int32_t nclasses, max_score;
+  // Publication number: a warp keeps the matrices it copied for as long as
+  // its tasks come from the same publication (a later request can sit at
+  // the same arena addresses with other scores).
+  uint64_t uid;
 };
 
+// Lane types of a task (bits 24.. of Task::pair).
+enum : int32_t { kLaneI32 = 0, kLaneI16 = 1, kLaneI16Checked = 2 };
+
 struct Task {  // one pair of a request
-  int32_t req, pair;
+  int32_t req, pair;  // pair: index | lane type << 24
 };
 
 struct Ctl {  // device memory
@@ -119,6 +140,7 @@ class Loop {
   std::unique_ptr<PinBuf[]> stages_;  // per slot: the page-locked block the request is staged in
   bool running_ = false;
   unsigned long long tail_ = 0;  // tasks published so far
+  uint64_t published_ = 0;       // requests published so far
   int64_t launches_ = 0, idle_exits_ = 0;
   int64_t outstanding_ = 0;  // tasks published and not yet seen done
 };
