@@ -161,3 +161,31 @@ def test_consensus_line(tmp_path):
     F.write(str(fin), recs + [F.Record(">short", "short", "AAA")])
     r = subprocess.run([B.CLI, "-i", str(fin), "-o", str(fout), "--consensus"], capture_output=True, text=True)
     assert r.returncode == 1 and "equal length" in r.stderr
+
+
+def test_in_process_cpp_tool(tmp_path):
+    """The C++ tool of include/tweakseq_gb300_tool.hpp aligns in process
+    what the command does: gapped FASTA with the input's header lines, the
+    oracle's global alignment; in local mode whole rows around the oracle's
+    local core."""
+    from test_tool_cpp import build_tool_check
+    exe = build_tool_check(tmp_path)
+    rng = np.random.default_rng(43)
+    a = W.random_protein(rng, 310).tobytes().decode()
+    b, _ = W._mutate_proteins(rng, np.frombuffer(a.encode(), np.uint8), np.array([310]), np.array([0.5]), 0.05)
+    b = b.tobytes().decode()
+    fin, fout = tmp_path / "in.fa", tmp_path / "out.fa"
+    F.write(str(fin), [F.Record(">first one", "first", a[:40].lower() + "-" + a[40:]), F.Record(">second", "second", b)])
+    r = subprocess.run([exe, str(fin), str(fout)], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stderr
+    recs = F.read(str(fout))
+    assert [x.header for x in recs] == [">first one", ">second"]
+    want = O.align(a.encode(), b.encode())
+    assert (recs[0].sequence, recs[1].sequence) == (want.aln_a, want.aln_b)
+    r = subprocess.run([exe, str(fin), str(fout), "--local"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    _check_full_local_rows(F.read(str(fout)), a, b, O.align(a.encode(), b.encode(), O.BLOSUM62, 11, 1, True))
+    # An invalid residue is reported, not aligned.
+    F.write(str(fin), [F.Record(">x", "x", "ACD1E"), F.Record(">y", "y", "ACDE")])
+    r = subprocess.run([exe, str(fin), str(fout)], capture_output=True, text=True)
+    assert r.returncode != 0 and "invalid residue" in r.stdout

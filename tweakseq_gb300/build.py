@@ -38,7 +38,8 @@ def sources() -> list[str]:
 
 
 def _deps() -> list[str]:
-    return [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "tweakseq_gb300.h")]
+    return [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "tweakseq_gb300.h"),
+                                                                 os.path.join(ROOT, "include", "tweakseq_gb300_tool.hpp")]
 
 
 def up_to_date() -> bool:

@@ -14,7 +14,9 @@
 //                     own FASTA writer wraps at 80, FASTAFile.cpp:149-171);
 //                     with --local each row still holds its whole input
 //                     sequence: the unaligned flanks stand against gaps
-//                     around the aligned core (full_local_rows below);
+//                     around the aligned core (full_local_rows in
+//                     tweakseq_gb300_tool.hpp, which also holds the FASTA
+//                     reader and writer shared with the in-process tool);
 //   --all-vs-all   -> every unordered pair, one TSV line per pair: labels,
 //                     score, identical columns, columns, percent identity
 //                     (the distance input of a guide tree);
@@ -43,59 +45,15 @@
 #include <vector>
 
 #include "../../include/tweakseq_gb300.h"
+#include "../../include/tweakseq_gb300_tool.hpp"
 
 namespace {
 
-struct Record {
-  std::string header;  // the whole header line, '>' included
-  std::string label;
-  std::string residues;
-};
-
-bool read_fasta(std::istream &in, std::vector<Record> &out, std::string &err, bool verbatim) {
-  std::string line;
-  enum { kSeek, kComment, kSequence } state = kSeek;
-  while (std::getline(in, line)) {
-    // Trim like QString::trimmed.
-    size_t a = 0, b = line.size();
-    while (a < b && std::isspace(static_cast<unsigned char>(line[a]))) ++a;
-    while (b > a && std::isspace(static_cast<unsigned char>(line[b - 1]))) --b;
-    line = line.substr(a, b - a);
-    if (line.empty()) continue;
-    const char c = line[0];
-    if (c == '>' || c == ';') {
-      if (state == kComment && c == ';') continue;  // further comment lines
-      Record r;
-      r.header = line;
-      const size_t sp = line.find(' ', 1);
-      r.label = sp == std::string::npos ? line.substr(1) : line.substr(1, sp - 1);
-      out.push_back(r);
-      state = kComment;
-      continue;
-    }
-    if (state == kSeek) continue;
-    for (char ch : line) {
-      if (std::isspace(static_cast<unsigned char>(ch))) continue;
-      if (verbatim) {
-        out.back().residues.push_back(ch);
-        continue;
-      }
-      if (ch == '-' || ch == '.') continue;
-      out.back().residues.push_back(char(std::toupper(static_cast<unsigned char>(ch))));
-    }
-    state = kSequence;
-  }
-  if (out.empty()) {
-    err = "no FASTA records";
-    return false;
-  }
-  return true;
-}
-
-void write_wrapped(std::ostream &o, const std::string &header, const std::string &s) {
-  o << header << '\n';
-  for (size_t k = 0; k < s.size(); k += 80) o << s.substr(k, 80) << '\n';
-}
+using tsq_tool::full_local_rows;
+using tsq_tool::read_fasta;
+using tsq_tool::Record;
+using tsq_tool::status_name;
+using tsq_tool::write_wrapped;
 
 void usage() {
   std::fprintf(stderr,
@@ -120,31 +78,6 @@ std::string newick(const std::vector<tsq_tree_node> &nodes, const std::vector<Re
     text[size_t(n + t)] = "(" + text[size_t(nd.left)] + la + "," + text[size_t(nd.right)] + lb + ")";
   }
   return (n == 1 ? text[0] : text[size_t(2 * n - 2)]) + ";";
-}
-
-// Full-length rows of a local alignment: every residue of a and of b appears
-// in its row, in order, so that removing the gaps gives the input back.
-// Columns, left to right: a[0:a_begin] over gaps, gaps over b[0:b_begin],
-// the aligned core (aln_a over aln_b), a[a_end:] over gaps, gaps over
-// b[b_end:].  An empty local alignment (score 0, coordinates 0) gives a over
-// gaps followed by gaps over b.
-void full_local_rows(const std::string &a, const std::string &b, const tsq_result &r, std::string &row_a,
-                     std::string &row_b) {
-  const size_t ab = size_t(r.a_begin), ae = size_t(r.a_end), bb = size_t(r.b_begin), be = size_t(r.b_end);
-  const std::string core_a = r.aln_a ? r.aln_a : "", core_b = r.aln_b ? r.aln_b : "";
-  row_a = a.substr(0, ab) + std::string(bb, '-') + core_a + a.substr(ae) + std::string(b.size() - be, '-');
-  row_b = std::string(ab, '-') + b.substr(0, bb) + core_b + std::string(a.size() - ae, '-') + b.substr(be);
-}
-
-const char *status_name(int rc) {
-  switch (rc) {
-    case TSQ_E_INVALID_ARG: return "invalid argument";
-    case TSQ_E_INVALID_RESIDUE: return "invalid residue for the scoring matrix";
-    case TSQ_E_NOMEM: return "out of memory";
-    case TSQ_E_CUDA: return "CUDA error (no usable GPU?)";
-    case TSQ_E_TOO_LARGE: return "input too large";
-    default: return "error";
-  }
 }
 
 }  // namespace
