@@ -348,6 +348,24 @@ def run_ours(args):
     plain_s = time.perf_counter() - t0
     plain_gcups = plain_cells / plain_s / 1e9
     assert np.array_equal(plain_scores, res_dev.table["score"][:P])
+    # The same calls at the C ABI, as a C caller makes them: residue pointers
+    # into the input buffer, one parameter block and one tsq_result reused.
+    from tweakseq_gb300 import _native as N
+    L = N.lib()
+    c_params, keep_c_params = N.make_params(output="score")
+    c_res = N.Result()
+    base = ps.seqs.ctypes.data
+    args_c = [(base + int(ps.a_off[k]), int(ps.a_len[k]), base + int(ps.b_off[k]), int(ps.b_len[k]))
+              for k in range(P)]
+    c_scores = np.empty(P, dtype=np.int64)
+    pref, rref = ctypes.byref(c_params), ctypes.byref(c_res)
+    t0 = time.perf_counter()
+    for k, (pa, la, pb, lb) in enumerate(args_c):
+        if L.tsq_align_pair(pa, la, pb, lb, pref, rref):
+            raise RuntimeError("tsq_align_pair failed")
+        c_scores[k] = c_res.score
+    plain_c_s = time.perf_counter() - t0
+    assert np.array_equal(c_scores, res_dev.table["score"][:P])
 
     # ---- roofline of the fill ---------------------------------------------
     # Roofline denominator: the measured int16x2 DPX instruction rate, two
@@ -389,7 +407,8 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": "GCUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps, "api": "tsq_align_batch (pinned host residues in, host results out)"},
         "plain": {"gcups": plain_gcups, "pairs": P, "ms_per_pair": plain_s / P * 1e3,
-                  "api": "tsq_align_pair, one launch sequence per pair"},
+                  "api": "tsq_align_pair through the Python API (aligner.align_pair), one pair per call",
+                  "c_abi_gcups": plain_cells / plain_c_s / 1e9, "c_abi_ms_per_pair": plain_c_s / P * 1e3},
         "batched_over_plain": value / plain_gcups,
         "bitexact": bitexact,
         "gpu_launches": launches_per_step * args.steps,

@@ -266,6 +266,46 @@ def test_plain_equals_batch():
             int(bat.table["b_begin"][k]))
 
 
+@pytest.mark.parametrize("output", ["score", "identity", "alignment"])
+def test_one_pair_path_every_kind(output):
+    """tsq_align_pair's one-pair path against the oracle, on every kind of
+    pair it runs: empty sequences, int16x2 warp tasks, int32 warp tasks, the
+    CTA fill (long int32 pairs, among them W:W pairs past the proven int16
+    range, which it runs in int32 at once) and, with lane 'i16', the calls it
+    leaves to the batch engine.  Calls in a row reuse its buffers: sizes go
+    up and down."""
+    rng = np.random.default_rng(41)
+
+    def prot(n):
+        return W.random_protein(rng, n).tobytes()
+
+    cases = [(b"", prot(30)), (prot(25), b""), (b"", b""), (prot(1), prot(1)), (prot(300), prot(500)),
+             (prot(900), prot(40)), (b"W" * 2900, b"W" * 2900), (b"W" * 3100, b"W" * 3100),
+             (prot(3000), prot(2600)), (prot(64), prot(70))]
+    seqs, pairs = [], []
+    for a, b in cases:
+        seqs += [a, b]
+        pairs.append((len(seqs) - 2, len(seqs) - 1))
+    ps = W._pairset_from_lists(seqs, pairs)
+    omode = {"score": O.MODE_SCORE, "identity": O.MODE_IDENT, "alignment": O.MODE_ALIGN}[output]
+    for local in (False, True):
+        mode = "local" if local else "global"
+        if output == "alignment":
+            want, sa, sb = oracle_batch(ps, local, omode, strings=True)
+            fields = FIELDS
+        else:
+            want = oracle_batch(ps, local, omode)
+            fields = score_fields(local) if output == "score" else ident_fields(local)
+        for lane in ("auto", "i32", "i16"):
+            for k, (a, b) in enumerate(cases):
+                r = A.align_pair(a, b, mode=mode, output=output, lane=lane)
+                got = tuple(getattr(r, f) for f in fields)
+                exp = tuple(int(want[f][k]) for f in fields)
+                assert got == exp, (output, mode, lane, k, len(a), len(b))
+                if output == "alignment":
+                    assert (r.aln_a, r.aln_b) == (sa[k], sb[k]), (mode, lane, k)
+
+
 @pytest.mark.parametrize("local", [False, True])
 def test_int16_overflow_rerun_and_lane_choices(local):
     """Scores beyond int16: the checked int16x2 fill flags them and the int32

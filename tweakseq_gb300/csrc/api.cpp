@@ -16,6 +16,7 @@ namespace {
 // One cached engine object per host thread and device, so that repeated
 // plain or batch calls reuse their device buffers instead of allocating.
 struct ThreadCache {
+  tsq::PairPath pair_path;  // tsq_align_pair's one-pair path
   std::unique_ptr<tsq_batch> pair_engine;
   std::unique_ptr<tsq_batch> batch_engine;
   std::vector<std::unique_ptr<tsq_batch>> chunk_engines;  // chunks 1.. of a large call
@@ -312,9 +313,13 @@ int tsq_align_pair(const uint8_t *a, int32_t la, const uint8_t *b, int32_t lb, c
   return guarded([&]() -> int {
     if (!out || !p || la < 0 || lb < 0 || (la > 0 && !a) || (lb > 0 && !b)) return TSQ_E_INVALID_ARG;
     std::memset(out, 0, sizeof(*out));
+    ThreadCache &c = cache();
+    const int lean = tsq::pair_align(&c.pair_path, a, la, b, lb, p, out);
+    if (lean != tsq::kPairNotTaken) return lean;
+    // Calls the one-pair path leaves to the batch engine (forced checked
+    // int16x2 lanes, pairs beyond its limits, bad parameters).
     int dev = 0;
     if (current_device(nullptr, &dev)) return TSQ_E_CUDA;
-    ThreadCache &c = cache();
     if (!c.pair_engine || c.pair_dev != dev) {
       c.pair_engine.reset(new tsq_batch());
       c.pair_dev = dev;

@@ -208,9 +208,8 @@ int pow2ceil(int64_t x) {
   return 1 << (64 - __builtin_clzll(uint64_t(x - 1)));
 }
 
-constexpr int kR = 8;
-// Longest sequence the int32 kernels take: coordinates travel in 20 bits.
-constexpr int64_t kMaxLen = (1 << 20) - 1;
+constexpr int kR = kFillRows;
+constexpr int64_t kMaxLen = kMaxPairLen;
 
 // A small pool of host worker threads for the planner's per-pair passes,
 // started on first use and kept for the life of the process (spawning
@@ -414,6 +413,8 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
               const tsq_pair_desc *pairs, int64_t n, const tsq_params *p, const tsq_batch_opts *opts, bool plain,
               int64_t call_pairs, int64_t call_cells, bool segmented);
 int prepare_object(tsq_batch *b, const tsq_params *p, const tsq_batch_opts *opts, Scheme *sc, int *sms);
+}  // namespace
+
 // int16x2 fills exist for every output but local identity.
 bool lanes16_possible(int out_mode, bool local, int lane) {
   return lane != TSQ_LANE_I32 && !(out_mode == kOutIdent && local);
@@ -422,7 +423,74 @@ bool lanes16_possible(int out_mode, bool local, int lane) {
 int out_mode_of(const tsq_params *p) {
   return p->output == TSQ_OUT_ALIGNMENT ? kOutTrace : (p->output == TSQ_OUT_IDENTITY ? kOutIdent : kOutScore);
 }
-}  // namespace
+
+int check_params(const tsq_params *p) {
+  if (p->gap_open < 0 || p->gap_extend < 0 || p->gap_open > 1000000 || p->gap_extend > 1000000)
+    return TSQ_E_INVALID_ARG;
+  if (p->mode != TSQ_GLOBAL && p->mode != TSQ_LOCAL) return TSQ_E_INVALID_ARG;
+  if (p->output < TSQ_OUT_SCORE || p->output > TSQ_OUT_ALIGNMENT) return TSQ_E_INVALID_ARG;
+  if (p->lane < TSQ_LANE_AUTO || p->lane > TSQ_LANE_I32) return TSQ_E_INVALID_ARG;
+  return TSQ_OK;
+}
+
+// The value range the int32 kernels assume: every H, E, F stays above
+// -(3*open + (m+n+1)*ext + 128), which must be far from their "minus
+// infinity" (-2^29).  Identity counts travel in 16 bits, local maxima in 24
+// bits of the reduction key.
+int pair_limits(const tsq_params *p, const Scheme &sc, int out_mode, int32_t a_len, int32_t b_len) {
+  if (a_len > kMaxLen || b_len > kMaxLen) return TSQ_E_TOO_LARGE;
+  if (3 * int64_t(p->gap_open) + (int64_t(a_len) + b_len + 1) * p->gap_extend + 128 >= (int64_t(1) << 28))
+    return TSQ_E_TOO_LARGE;
+  if (out_mode == kOutIdent && int64_t(a_len) + b_len > 65535) return TSQ_E_TOO_LARGE;
+  if (p->mode == TSQ_LOCAL && int64_t(std::max(sc.max_score, 0)) * std::min(a_len, b_len) >= (1 << 23))
+    return TSQ_E_TOO_LARGE;
+  return TSQ_OK;
+}
+
+// int16x2 range of a pair: the upper bound max_score * min(m, n) (no
+// overflow check needed) and the lower bound -(3*open + (m + 512 + n +
+// 1)*ext + open + ext + 128 + |min|), 512 being the most padding rows a pass
+// can add, against the int16 kernels' minus infinity (-32000); the int16x2
+// kernel also subtracts open + ext from values at this bound (T and XO),
+// which must stay above -32768.
+Range16 range16(const tsq_params *p, const Scheme &sc, int32_t a_len, int32_t b_len) {
+  const int64_t go = p->gap_open, ge = p->gap_extend;
+  const int64_t smax = std::max(sc.max_score, 0), sneg = std::max<int64_t>(0, -int64_t(sc.min_score));
+  const int64_t lowest = 3 * go + (int64_t(a_len) + 512 + b_len + 1) * ge + go + ge + 128 + sneg;
+  Range16 r;
+  r.lower = lowest + go + ge < 31000 && ge <= 700 && b_len <= 65535;
+  r.upper = smax * std::min(a_len, b_len) + smax < 32767;
+  return r;
+}
+
+int collect_one(const ResultDev &d, const char *rows, int64_t cap, tsq_result &o) {
+  o.score = d.score;
+  o.a_begin = d.a_begin;
+  o.a_end = d.a_end;
+  o.b_begin = d.b_begin;
+  o.b_end = d.b_end;
+  o.n_ident = d.n_ident;
+  o.n_cols = d.n_cols;
+  o.status = d.status;
+  o.aln_a = o.aln_b = nullptr;
+  if (!rows) return TSQ_OK;
+  const int64_t L = d.n_cols;
+  if (L < 0 || L > cap) return TSQ_E_CUDA;
+  o.aln_a = static_cast<char *>(std::malloc(size_t(L) + 1));
+  o.aln_b = static_cast<char *>(std::malloc(size_t(L) + 1));
+  if (!o.aln_a || !o.aln_b) {
+    std::free(o.aln_a);
+    std::free(o.aln_b);
+    o.aln_a = o.aln_b = nullptr;
+    return TSQ_E_NOMEM;
+  }
+  // The walker writes each row right-aligned in cap bytes.
+  std::memcpy(o.aln_a, rows + cap - L, size_t(L));
+  std::memcpy(o.aln_b, rows + 2 * cap - L, size_t(L));
+  o.aln_a[L] = 0;
+  o.aln_b[L] = 0;
+  return TSQ_OK;
+}
 
 int batch_plan(tsq_batch *b, const uint8_t *seqs, int64_t seqs_len, const tsq_pair_desc *pairs, int64_t n,
                const tsq_params *p, const tsq_batch_opts *opts, bool plain) {
@@ -496,12 +564,9 @@ namespace {
 // Checks the parameters, builds the scheme and readies the object for a new
 // plan on its device: drops an old graph, (re)creates its streams and events.
 int prepare_object(tsq_batch *b, const tsq_params *p, const tsq_batch_opts *opts, Scheme *sc, int *sms) {
-  if (p->gap_open < 0 || p->gap_extend < 0 || p->gap_open > 1000000 || p->gap_extend > 1000000)
-    return TSQ_E_INVALID_ARG;
-  if (p->mode != TSQ_GLOBAL && p->mode != TSQ_LOCAL) return TSQ_E_INVALID_ARG;
-  if (p->output < TSQ_OUT_SCORE || p->output > TSQ_OUT_ALIGNMENT) return TSQ_E_INVALID_ARG;
-  if (p->lane < TSQ_LANE_AUTO || p->lane > TSQ_LANE_I32) return TSQ_E_INVALID_ARG;
-  int rc = build_scheme(p, sc);
+  int rc = check_params(p);
+  if (rc) return rc;
+  rc = build_scheme(p, sc);
   if (rc) return rc;
 
   int dev = opts && opts->device >= 0 ? opts->device : -1;
@@ -586,16 +651,8 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
         rc = TSQ_E_INVALID_ARG;
       else if (d.a_off > seqs_len - d.a_len || d.b_off > seqs_len - d.b_len)
         rc = TSQ_E_INVALID_ARG;
-      else if (d.a_len > kMaxLen || d.b_len > kMaxLen)
-        rc = TSQ_E_TOO_LARGE;
-      else if (3 * int64_t(p->gap_open) + (int64_t(d.a_len) + d.b_len + 1) * p->gap_extend + 128 >=
-               (int64_t(1) << 28))
-        rc = TSQ_E_TOO_LARGE;
-      else if (b->out_mode == kOutIdent && int64_t(d.a_len) + d.b_len > 65535)
-        rc = TSQ_E_TOO_LARGE;
-      // Local maxima travel in 24 bits of the reduction key.
-      else if (p->mode == TSQ_LOCAL && int64_t(std::max(sc.max_score, 0)) * std::min(d.a_len, d.b_len) >= (1 << 23))
-        rc = TSQ_E_TOO_LARGE;
+      else
+        rc = pair_limits(p, sc, b->out_mode, d.a_len, d.b_len);
       if (rc != TSQ_OK) {
         v.bad_at = k;
         v.rc = rc;
@@ -646,13 +703,8 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   }
 
   // ---- lane types, shapes and order (one parallel pass over the pairs) ----
-  // Score fills run in int16x2 when the pair's values provably fit: the
-  // upper bound max_score * min(m, n) (unchecked kernel) and the lower
-  // bound -(3*open + (m + 512 + n + 1)*ext + open + ext + 128 + |min|),
-  // 512 being the most padding rows a pass can add, against the int16
-  // kernels' minus infinity (-32000); the int16x2 kernel also subtracts
-  // open + ext from values at this bound (T and XO), which must stay above
-  // -32768.  Pairs with the lower bound but not the upper one run the
+  // Fills run in int16x2 when the pair's values provably fit (range16: both
+  // bounds).  Pairs with the lower bound but not the upper one run the
   // overflow-checked int16x2 kernel and are re-run in int32 if flagged;
   // everything else runs in int32.
   //
@@ -710,9 +762,7 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   {
     const double lanes = double(sms) * 24.0 * 32.0;
     const double cta_budget = std::max(20000.0, plain ? 0.0 : double(shape_cells) / (lanes * kR));
-    const int64_t go = p->gap_open, ge = p->gap_extend;
     const bool try16 = lanes16_possible(b->out_mode, b->local, p->lane);
-    const int64_t smax = std::max(sc.max_score, 0), sneg = std::max<int64_t>(0, -int64_t(sc.min_score));
     parallel_for(n, [&](int64_t lo, int64_t hi, int slot) {
       ShapePart sp;
       for (int64_t k = lo; k < hi; ++k) {
@@ -723,10 +773,8 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
         TunedChoice tc;
         const bool tuned = ch.use_table && !ch.force.shape && tune_table_pick(b->out_mode, pd.a_len, pd.b_len, &tc);
         if (try16 && !(tuned && tc.sh.i16 == 0)) {
-          const int64_t lowest = 3 * go + (int64_t(pd.a_len) + 512 + pd.b_len + 1) * ge + go + ge + 128 + sneg;
-          const bool lower_ok = lowest + go + ge < 31000 && ge <= 700 && pd.b_len <= 65535;
-          const bool upper_ok = smax * std::min(pd.a_len, pd.b_len) + smax < 32767;
-          if (lower_ok) lt = (upper_ok && p->lane == TSQ_LANE_AUTO) ? 1 : 2;
+          const Range16 r16 = range16(p, sc, pd.a_len, pd.b_len);
+          if (r16.lower) lt = (r16.upper && p->lane == TSQ_LANE_AUTO) ? 1 : 2;
         }
         if (lt == 0 && pd.a_len > 0 && pd.b_len > 0) {
           const double steps32 = double((pd.a_len + 255) / 256) * double(pd.b_len + 31);
@@ -1289,39 +1337,13 @@ int batch_collect(tsq_batch *b, int64_t begin, int64_t count, tsq_result *out, c
     const int64_t k = begin + q;
     tsq_result &o = dst ? out[dst[q]] : out[q];
     const ResultDev &d = r[k];
-    o.score = d.score;
-    o.a_begin = d.a_begin;
-    o.a_end = d.a_end;
-    o.b_begin = d.b_begin;
-    o.b_end = d.b_end;
-    o.n_ident = d.n_ident;
-    o.n_cols = d.n_cols;
-    o.status = d.status;
-    o.aln_a = o.aln_b = nullptr;
-    if (d.status != TSQ_OK) {
-      // A residue error is the caller's; anything else is the library's.
-      if (rc == TSQ_OK || d.status != TSQ_E_INVALID_RESIDUE) rc = d.status;
-      continue;
-    }
-    if (b->out_mode == kOutTrace) {
-      const PairDev &pd = b->pairs_h[size_t(k)];
-      const int64_t cap = int64_t(pd.a_len) + pd.b_len;
-      const int64_t L = d.n_cols;
-      if (L < 0 || L > cap) return TSQ_E_CUDA;
-      const char *base = b->aln_h.as<char>() + b->aln_off_h[size_t(k)];
-      o.aln_a = static_cast<char *>(std::malloc(size_t(L) + 1));
-      o.aln_b = static_cast<char *>(std::malloc(size_t(L) + 1));
-      if (!o.aln_a || !o.aln_b) {
-        std::free(o.aln_a);
-        std::free(o.aln_b);
-        o.aln_a = o.aln_b = nullptr;
-        return TSQ_E_NOMEM;
-      }
-      std::memcpy(o.aln_a, base + cap - L, size_t(L));
-      std::memcpy(o.aln_b, base + 2 * cap - L, size_t(L));
-      o.aln_a[L] = 0;
-      o.aln_b[L] = 0;
-    }
+    const bool rows = b->out_mode == kOutTrace && d.status == TSQ_OK;
+    const PairDev &pd = b->pairs_h[size_t(k)];
+    const int e = collect_one(d, rows ? b->aln_h.as<char>() + b->aln_off_h[size_t(k)] : nullptr,
+                              int64_t(pd.a_len) + pd.b_len, o);
+    if (e) return e;
+    // A residue error is the caller's; anything else is the library's.
+    if (d.status != TSQ_OK && (rc == TSQ_OK || d.status != TSQ_E_INVALID_RESIDUE)) rc = d.status;
   }
   return rc;
 }

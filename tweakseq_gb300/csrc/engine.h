@@ -230,6 +230,45 @@ int batch_collect(tsq_batch *b, int64_t begin, int64_t count, tsq_result *out, c
 // Parallel on the worker pool; `bin` is scratch.
 int64_t cost_order(const tsq_pair_desc *pairs, int64_t n, std::vector<uint8_t> &bin, tsq_pair_desc *out_pairs,
                    int32_t *out_index);
+
+// ---- per-pair rules shared by the planner and the one-pair path ----------
+// Rows per lane of every fill.
+constexpr int kFillRows = 8;
+// Longest sequence the int32 kernels take: coordinates travel in 20 bits.
+constexpr int64_t kMaxPairLen = (1 << 20) - 1;
+int out_mode_of(const tsq_params *p);
+bool lanes16_possible(int out_mode, bool local, int lane);
+// TSQ_E_INVALID_ARG for gap costs, mode, output or lane out of range.
+int check_params(const tsq_params *p);
+// TSQ_E_TOO_LARGE for a pair beyond the kernels' value and length ranges.
+int pair_limits(const tsq_params *p, const Scheme &sc, int out_mode, int32_t a_len, int32_t b_len);
+// Whether a pair's int16x2 values provably stay in range: lower (its most
+// negative values above the kernels' minus infinity) and upper (its best
+// score below 32767, so the fill needs no overflow check).
+struct Range16 {
+  bool lower = false, upper = false;
+};
+Range16 range16(const tsq_params *p, const Scheme &sc, int32_t a_len, int32_t b_len);
+// Copies a result record into o and, when rows is set (an alignment whose
+// status is OK), its two rows from the walker's output of 2 * cap bytes.
+// Returns TSQ_OK, or TSQ_E_CUDA / TSQ_E_NOMEM when the rows cannot be taken.
+int collect_one(const ResultDev &d, const char *rows, int64_t cap, tsq_result &o);
+
+// The plain form's one-pair path (pair.cpp).  One object per host thread.
+struct PairPath {
+  int device = -1;
+  int sms = 0;
+  cudaStream_t stream = nullptr;
+  DevBuf dev;       // upload block | codes | class codes | result | rows | boundary | planes
+  PinBuf up, down;  // the upload block; the result record and rows coming back
+  void reset();     // frees the buffers and the stream (device change)
+  ~PairPath() { reset(); }
+};
+// A tsq_align_pair call the one-pair path does not take returns this; the
+// caller then runs the batch engine, which owns those cases' checks.
+constexpr int kPairNotTaken = -1000;
+int pair_align(PairPath *pp, const uint8_t *a, int32_t la, const uint8_t *b, int32_t lb, const tsq_params *p,
+               tsq_result *out);
 int64_t batch_device_bytes(const tsq_batch *b);
 // Returns the memory the engine's stream-ordered pool keeps mapped on a
 // device but does not use (before a call sizes itself by the free memory).
