@@ -463,6 +463,53 @@ def test_long_pairs_on_the_cta_fill_all_outputs(local):
     assert (r.score, r.aln_a, r.aln_b) == (int(want["score"][2]), sa[2], sb[2])
 
 
+@pytest.mark.parametrize("output", ["score", "alignment"])
+def test_int16_cta_fill_rebased_values(output):
+    """Long global pairs on the CTA fill in int16x2 lanes, whose values are
+    kept relative to a moving base: scores far past the int16 range upwards
+    (W:W, 176,000) and downwards, a 4,000-residue gap, a 40-column pair (no
+    interior steps), 513 rows (a one-row second pass), 17 passes (the
+    wrap-around row), BLOSUM62 (23 classes, 16 warps) and DNA, against the
+    oracle; gap costs at the bound (open + ext + max score = 40) and past it
+    (the int32 CTA fill).  The plain form of a long pair takes the same
+    kernel."""
+    rng = np.random.default_rng(61)
+
+    def prot(n):
+        return W.random_protein(rng, n).tobytes()
+
+    big = prot(20000)
+    prot_cases = [(b"W" * 16000, b"W" * 16000), (prot(16000), prot(15000)), (big, big[:8000] + big[12000:]),
+                  (prot(80000), prot(40)), (prot(513), prot(40000)), (prot(8193), prot(23000))]
+    d = W.DNA_LETTERS[rng.integers(0, 4, 30000)]
+    dna_cases = [(d.tobytes(), W._mutate_dna(rng, d, 0.05, 0.01, 3.0)[:29000].tobytes()),
+                 (W.DNA_LETTERS[rng.integers(0, 4, 20000)].tobytes(),
+                  W.DNA_LETTERS[rng.integers(0, 4, 20000)].tobytes())]
+    omode = O.MODE_ALIGN if output == "alignment" else O.MODE_SCORE
+    fields = FIELDS if output == "alignment" else ("score",)
+    for cases, matrix, gaps in ((prot_cases, "blosum62", ((11, 1), (25, 4), (27, 4))),
+                                (dna_cases, "dna", ((5, 2),))):
+        seqs, pairs = [], []
+        for a, b in cases:
+            seqs += [a, b]
+            pairs.append((len(seqs) - 2, len(seqs) - 1))
+        ps = W._pairset_from_lists(seqs, pairs)
+        which = O.DNA if matrix == "dna" else O.BLOSUM62
+        for go, ge in gaps:
+            want = O.batch(ps.seqs, ps.a_off, ps.a_len, ps.b_off, ps.b_len, which, go, ge, False, omode, 0,
+                           output == "alignment")
+            if output == "alignment":
+                want, sa, sb = want
+            got = A.align_batch(ps, matrix=matrix, gap_open=go, gap_extend=ge, output=output)
+            assert_same(got, want, fields, f"{matrix} {go}/{ge}")
+            if output == "alignment":
+                assert got.aln_a == sa and got.aln_b == sb, f"{matrix} {go}/{ge}"
+            r = A.align_pair(*ps.pair(len(ps) - 1), matrix=matrix, gap_open=go, gap_extend=ge, output=output)
+            assert r.score == int(want["score"][len(ps) - 1])
+            if output == "alignment":
+                assert (r.aln_a, r.aln_b) == (sa[-1], sb[-1])
+
+
 def test_alignment_batch_in_waves(monkeypatch):
     """An alignment batch whose traceback planes exceed the memory budget
     runs in waves (largest pairs first); every result matches the

@@ -712,9 +712,12 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   // or 8 warps of a CTA):
   // those whose sweep on one 32-lane group -- ceil(m/256) bands of n+31
   // steps -- would outlast the batch's balanced per-lane work (or, alone,
-  // 20,000 steps).
+  // 20,000 steps).  Under the automatic lane type, global score and
+  // traceback pairs take the CTA fill in int16x2 lanes with rebased values
+  // (fill_cta16.cuh) when open + ext + max_score <= 40.
   //
-  // Order: lane type (CTA, checked int16x2, int16x2, int32), then lane
+  // Order: lane type (CTA int16x2, CTA int32, checked int16x2, int16x2,
+  // int32), then lane
   // width, then bands and columns descending, then input order -- one
   // 44-bit key, sorted by a stable LSD radix sort (O(n): the plan of an
   // 8M-pair batch must not cost seconds).
@@ -763,6 +766,10 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
     const double lanes = double(sms) * 24.0 * 32.0;
     const double cta_budget = std::max(20000.0, plain ? 0.0 : double(shape_cells) / (lanes * kR));
     const bool try16 = lanes16_possible(b->out_mode, b->local, p->lane);
+    // Long pairs take the CTA fill in int16x2 lanes (rebased values) where
+    // the scheme allows it and the lane type is automatic.
+    const bool cta16 = p->lane == TSQ_LANE_AUTO && cta16_supported(b->out_mode, b->local, sc, p->gap_open,
+                                                                     p->gap_extend);
     parallel_for(n, [&](int64_t lo, int64_t hi, int slot) {
       ShapePart sp;
       for (int64_t k = lo; k < hi; ++k) {
@@ -778,13 +785,13 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
         }
         if (lt == 0 && pd.a_len > 0 && pd.b_len > 0) {
           const double steps32 = double((pd.a_len + 255) / 256) * double(pd.b_len + 31);
-          if (steps32 > cta_budget || ch.force.cta || (tuned && tc.cta)) lt = 3;
+          if (steps32 > cta_budget || ch.force.cta || (tuned && tc.cta)) lt = cta16 ? 4 : 3;
         }
         lsel[size_t(k)] = lt;
         sp.n_checked += lt == 2;
         const int rows_per_lane = (lt == 1 || lt == 2) ? 2 * kR : kR;
         Shape shp = ch.pick(pd.a_len, pd.b_len, rows_per_lane);
-        if (lt == 3) shp = Shape{32, kR, 0};  // one 32-lane group per warp of the CTA
+        if (lt >= 3) shp = Shape{32, kR, 0};  // one 32-lane group per warp of the CTA
         shp.i16 = 0;
         if (!shape_supported(shp, b->out_mode, b->local)) sp.bad_shape = true;
         gsel[size_t(k)] = shp.G;
@@ -797,7 +804,9 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
         ps.cost[size_t(k)] = int64_t(bands(k)) * steps(k);
         sp.max_bands = std::max(sp.max_bands, bandk);
         sp.max_cols = std::max(sp.max_cols, colk);
-        static const uint64_t kLaneRank[4] = {3, 2, 1, 0};  // CTA, checked int16x2, int16x2, int32
+        // Ranks of the lane types 0..4, in launch order: CTA int16x2, CTA
+        // int32, checked int16x2, int16x2, int32.
+        static const uint64_t kLaneRank[5] = {4, 3, 2, 1, 0};
         // Provisional key; packed to the bits the batch needs below.
         recs[size_t(k)] = SortRec{(kLaneRank[lt] << 42) | (uint64_t(gi) << 40) | (uint64_t(bandk) << 20) |
                                       uint64_t(colk),
@@ -824,7 +833,7 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
       const uint64_t top = r.key >> 40, bandk = (r.key >> 20) & ((1u << 20) - 1), colk = r.key & ((1u << 20) - 1);
       r.key = (top << (wb + wc)) | ((uint64_t(max_bands) - bandk) << wc) | (uint64_t(max_cols) - colk);
     }
-    radix_sort(recs, ps.tmp, 4 + wb + wc);
+    radix_sort(recs, ps.tmp, 5 + wb + wc);  // 3 bits of lane rank, 2 of lane width
   }
   ps.order.resize(size_t(n));
   ps.s_lt.resize(size_t(n));
@@ -859,15 +868,15 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
       ++e;
     }
     if (lt == 2) checked_begin = int32_t(s);
-    if (lt == 3) {
+    if (lt >= 3) {
       // One long pair per CTA; the CTAs pull pairs longest first.
       Launch L;
       L.R = kR;
-      L.i16 = 0;
+      L.i16 = lt == 4 ? 1 : 0;  // int16x2 lanes with rebased values
       L.cta = true;
       L.task_begin = int32_t(s);
       L.n_wtasks = int32_t(e - s);
-      const int max_blocks = cta_blocks(b->out_mode, b->local);
+      const int max_blocks = lt == 4 ? cta16_blocks(b->out_mode, sc.nclasses) : cta_blocks(b->out_mode, b->local);
       if (max_blocks <= 0) return TSQ_E_CUDA;
       L.blocks = int32_t(std::max<int64_t>(1, std::min<int64_t>(max_blocks, e - s)));
       L.bnd_cols = ((cols + 31) / 32 + 1) * 32;
@@ -1056,6 +1065,7 @@ cudaError_t record(tsq_batch *b, int k) {
 
 // Fill launch names for the trace ranges: [i16][out_mode].
 const char *fill_range_name(const Launch &L, int out_mode) {
+  if (L.cta && L.i16) return out_mode == kOutTrace ? "fill_cta16 trace" : "fill_cta16 score";
   if (L.cta) return out_mode == kOutTrace ? "fill_cta trace" : (out_mode == kOutIdent ? "fill_cta identity" : "fill_cta score");
   if (L.rerun) return "fill_i32 re-run of int16 overflows";
   if (L.i16 == 1) return "fill_i16 score";
@@ -1112,7 +1122,14 @@ int enqueue_run(tsq_batch *b) {
       a.plane_off = b->plane_off.as<int64_t>();
       a.max_score = b->scheme.max_score;
       a.spin_limit = b->wait_polls;
-      TSQ_TRY(launch_cta(b->out_mode, b->local, a, L.blocks, b->side));
+      if (L.i16) {
+        a.ccodes = ccodes_dev(b);
+        a.cmatrix = b->cmatrix.as<int8_t>();
+        a.nclasses = b->scheme.nclasses;
+        TSQ_TRY(launch_cta16(b->out_mode, a, L.blocks, b->side));
+      } else {
+        TSQ_TRY(launch_cta(b->out_mode, b->local, a, L.blocks, b->side));
+      }
       continue;
     }
     if (L.rerun) {

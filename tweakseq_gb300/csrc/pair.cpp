@@ -12,8 +12,9 @@
 //
 // Lane choice: the batch planner's, with one difference.  A pair whose
 // int16x2 range is not proven (range16: lower bound only) runs in int32 at
-// once, where the planner would run the overflow-checked int16x2 fill and
-// re-run a flagged pair in int32 -- a second round trip for one pair.
+// once (or, when long, on the int16x2 CTA fill), where the planner would
+// run the overflow-checked int16x2 fill and re-run a flagged pair in int32
+// -- a second round trip for one pair.
 // Scores, coordinates and rows are the same in every lane type.  Calls
 // that force the checked int16x2 lane (TSQ_LANE_I16) and pairs outside
 // pair_limits go to the batch engine (kPairNotTaken), which owns those
@@ -102,7 +103,8 @@ int pair_align(PairPath *pp, const uint8_t *a, int32_t la, const uint8_t *b, int
   } sync_on_exit{st};
 
   // ---- lane type and shape: the planner's rules for a lone pair ----------
-  // 0 int32 warp task, 1 int16x2 warp task, 3 CTA fill (int32).
+  // 0 int32 warp task, 1 int16x2 warp task, 3 CTA fill (int32), 4 CTA fill
+  // (int16x2, rebased values).
   int lt = 0;
   if (lanes16_possible(out_mode, local, p->lane)) {
     const Range16 r16 = range16(p, sc, la, lb);
@@ -110,7 +112,8 @@ int pair_align(PairPath *pp, const uint8_t *a, int32_t la, const uint8_t *b, int
   }
   if (lt == 0 && la > 0 && lb > 0) {
     const double steps32 = double((la + 255) / 256) * double(lb + 31);
-    if (steps32 > 20000.0) lt = 3;
+    if (steps32 > 20000.0)
+      lt = p->lane == TSQ_LANE_AUTO && cta16_supported(out_mode, local, sc, p->gap_open, p->gap_extend) ? 4 : 3;
   }
   ShapeChooser ch;
   ch.out_mode = out_mode;
@@ -119,14 +122,15 @@ int pair_align(PairPath *pp, const uint8_t *a, int32_t la, const uint8_t *b, int
   ch.npairs = 1;
   ch.prepare();
   Shape shp = ch.pick(la, lb, lt == 1 ? 2 * kFillRows : kFillRows);
-  if (lt == 3) shp = Shape{32, kFillRows, 0};
+  if (lt >= 3) shp = Shape{32, kFillRows, 0};
   if (!shape_supported(shp, out_mode, local)) return kPairNotTaken;
-  const int i16 = lt == 1 ? 1 : 0;
+  const int i16 = lt == 1 || lt == 4 ? 1 : 0;  // class codes and class matrix in use
 
   // Resident blocks of the kernel: the query also opts it into its shared
   // memory (answered from a cache after the first call).
-  const int blocks_avail = lt == 3 ? cta_blocks(out_mode, local)
-                                   : fill_blocks(kFillRows, i16, out_mode, local, i16 ? sc.nclasses : kLetters);
+  const int blocks_avail = lt == 4   ? cta16_blocks(out_mode, sc.nclasses)
+                           : lt == 3 ? cta_blocks(out_mode, local)
+                                     : fill_blocks(kFillRows, i16, out_mode, local, i16 ? sc.nclasses : kLetters);
   if (blocks_avail <= 0) return TSQ_E_CUDA;
 
   // ---- device layout ---------------------------------------------------
@@ -140,7 +144,7 @@ int pair_align(PairPath *pp, const uint8_t *a, int32_t la, const uint8_t *b, int
   const int64_t off_bnd = off_res + align256(down_bytes);
   const int32_t bnd_cols = ((std::max(lb, 1) + 31) / 32 + 1) * 32;
   const int64_t bnd_bytes =
-      lt == 3 ? int64_t(bnd_cols) * int64_t(cta_bnd_entry_bytes(out_mode))
+      lt >= 3 ? int64_t(bnd_cols) * int64_t(cta_bnd_entry_bytes(out_mode))
               : int64_t(fill_threads_for(i16) / 32) * 8 * bnd_cols * int64_t(fill_bnd_entry_bytes(i16, out_mode));
   const int64_t off_planes = off_bnd + align256(bnd_bytes);
   const int64_t plane_total = trace ? plane_bytes(la, lb, Shape{shp.G, shp.R, 0}) : 0;
@@ -200,7 +204,9 @@ int pair_align(PairPath *pp, const uint8_t *a, int32_t la, const uint8_t *b, int
     fa.cmatrix = reinterpret_cast<const int8_t *>(d + kOffCmatrix);
     fa.nclasses = sc.nclasses;
   }
-  if (lt == 3) {
+  if (lt == 4) {
+    PAIR_TRY(launch_cta16(out_mode, fa, 1, st));
+  } else if (lt == 3) {
     PAIR_TRY(launch_cta(out_mode, local, fa, 1, st));
   } else {
     PAIR_TRY(launch_fill(kFillRows, i16, out_mode, local, fa, 1, st));
