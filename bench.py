@@ -775,13 +775,13 @@ def traceback_uneven(O, A, W, cores, sample=2000):
         "checked": f"{sample} seeded pairs byte for byte: score, coordinates, identity, both gapped strings"}
 
 
-def long_pair_kernels(ps, per_sm=2):
+def long_pair_kernels(ps, per_sm=1):
     """Rooflines of the long-pair kernels: a device-resident batch of the
-    first long DNA pairs, per_sm of them per SM (the CTA fill's residency,
-    so that every SM holds that many pairs at once) as far as their
+    first long DNA pairs, per_sm of them per SM (the CTA fill's residency:
+    one 16-warp CTA per SM, so that every SM holds one pair) as far as their
     traceback planes fit in 40 % of the free HBM (at most 120 GB): the CTA
-    traceback fill, then one walker warp per pair, timed by the batch's own
-    events."""
+    traceback fill in int16x2 lanes, then one walker warp per pair, timed by
+    the batch's own events."""
     import torch
 
     from tweakseq_gb300 import aligner as A
@@ -803,9 +803,9 @@ def long_pair_kernels(ps, per_sm=2):
     fill_s = float(np.median(fills)) * 1e-3
     walk_s = float(np.median(rest)) * 1e-3
     gc = sub.cells / fill_s / 1e9
-    peak = dpx_cell_peak(False)
+    peak = dpx_cell_peak(True)
     hbm, hbm_src = hbm_peak()
-    rec = traffic_record("fill_cta_long_dna_32")
+    rec = traffic_record("fill_cta16_long_dna_32")
     traffic = rec["dram_bytes_per_launch"] * sub.cells / rec["cells"] if rec else None
     plane_gbs = 0.5 * sub.cells / fill_s / 1e9
     # Walker bytes: the nibble of each walked cell, both gapped rows written
@@ -814,12 +814,13 @@ def long_pair_kernels(ps, per_sm=2):
     walk_bytes = float((0.5 * cols + 2 * cols).sum() + sub.a_len.sum() + sub.b_len.sum())
     return {
         "pairs": n_pairs, "cells": sub.cells,
-        "fill_cta_kernel": {
+        "fill_cta16_kernel": {
             "fill_ms": fill_s * 1e3,
             "roofline": {"bound": "int", "achieved": gc, "peak": peak, "unit": "Gcell/s", "frac": gc / peak,
                          "traffic": traffic, "traffic_source": "ncu DRAM bytes of a 32-pair launch, scaled by cells",
-                         "peak_source": "measured live: tsq_probe_dpx int32 rate / 4 DPX instructions per cell",
-                         "note": f"{n_pairs} pairs, one CTA each, at most {per_sm} per SM"},
+                         "peak_source": "measured live: tsq_probe_dpx int16x2 rate x 2 cells / 4 DPX instructions "
+                                        "per cell",
+                         "note": f"{n_pairs} pairs, one 16-warp CTA each, at most {per_sm} per SM"},
             "plane_writes": {"bound": "hbm", "achieved": plane_gbs, "peak": hbm, "unit": "GB/s",
                              "frac": plane_gbs / hbm, "bytes_per_cell": 0.5, "peak_source": hbm_src}},
         "walk_warp_kernel": {
