@@ -637,6 +637,14 @@ def configs_leg(c3_pairs=12):
     t0 = time.perf_counter()
     res = A.align_batch(ps, matrix="dna", gap_open=5, gap_extend=2, output="alignment")
     c3_s = time.perf_counter() - t0
+    # The same call with int32 lanes throughout (the int32 CTA fill for the
+    # long pairs); every result must equal the default run's.
+    t0 = time.perf_counter()
+    res32 = A.align_batch(ps, matrix="dna", gap_open=5, gap_extend=2, output="alignment", lane="i32")
+    c3_i32_s = time.perf_counter() - t0
+    same32 = bool(all(np.array_equal(res32.table[f], res.table[f]) for f in ("score", "n_ident", "n_cols"))
+                  and res32.aln_a == res.aln_a and res32.aln_b == res.aln_b)
+    del res32
     # The longest pair of the workload plus a seeded sample, compared with
     # the oracle byte for byte (its direction matrix takes a byte per cell,
     # so its threads are bounded by the host's free memory).
@@ -663,6 +671,10 @@ def configs_leg(c3_pairs=12):
     out["long_dna_pairs_1000"] = {
         "pairs": len(ps), "cells": ps.cells, "output": "alignment (global, +2/-3, gap 5/2)",
         "e2e_gcups": ps.cells / c3_s / 1e9, "seconds": c3_s,
+        "e2e_gcups_int32_lanes": ps.cells / c3_i32_s / 1e9, "int32_lanes_equal": same32,
+        "lanes": "e2e_gcups: the long-pair fill in int16x2 lanes whose values each warp keeps relative to a "
+                 "moving int32 base (exact: the int32 recurrence's integers, proven in range); "
+                 "e2e_gcups_int32_lanes: the same call on int32 lanes (lane i32), every result compared",
         "api": "tsq_align_batch, host buffers; waves sized to free HBM, largest pairs first",
         "plain_gcups": float(all_cells[plain_idx].sum()) / plain_s / 1e9,
         "plain_pairs": len(plain_idx),
