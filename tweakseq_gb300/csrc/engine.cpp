@@ -714,7 +714,9 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   // steps -- would outlast the batch's balanced per-lane work (or, alone,
   // 20,000 steps).  Under the automatic lane type, global score and
   // traceback pairs take the CTA fill in int16x2 lanes with rebased values
-  // (fill_cta16.cuh) when open + ext + max_score <= 40.
+  // (fill_cta16.cuh) when open + ext + max_score <= 40: the long int32
+  // pairs, and the int16x2 pairs whose sweep on one 32-lane group --
+  // ceil(m/512) passes of n+63 steps -- exceeds the same budget.
   //
   // Order: lane type (CTA int16x2, CTA int32, checked int16x2, int16x2,
   // int32), then lane
@@ -786,6 +788,12 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
         if (lt == 0 && pd.a_len > 0 && pd.b_len > 0) {
           const double steps32 = double((pd.a_len + 255) / 256) * double(pd.b_len + 31);
           if (steps32 > cta_budget || ch.force.cta || (tuned && tc.cta)) lt = cta16 ? 4 : 3;
+        } else if (lt != 0 && cta16 && !ch.force.shape) {
+          // An int16x2 pair whose sweep on one 32-lane group -- ceil(m/512)
+          // passes of n+63 steps -- would be the batch's tail (and, when
+          // checked, might need an int32 re-run on one warp as well).
+          const double steps16 = double((pd.a_len + 511) / 512) * double(pd.b_len + 63);
+          if (steps16 > cta_budget) lt = 4;
         }
         lsel[size_t(k)] = lt;
         sp.n_checked += lt == 2;

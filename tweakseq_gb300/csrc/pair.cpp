@@ -110,10 +110,13 @@ int pair_align(PairPath *pp, const uint8_t *a, int32_t la, const uint8_t *b, int
     const Range16 r16 = range16(p, sc, la, lb);
     if (r16.lower && r16.upper && p->lane == TSQ_LANE_AUTO) lt = 1;
   }
+  const bool cta16 = p->lane == TSQ_LANE_AUTO && cta16_supported(out_mode, local, sc, p->gap_open, p->gap_extend);
   if (lt == 0 && la > 0 && lb > 0) {
     const double steps32 = double((la + 255) / 256) * double(lb + 31);
-    if (steps32 > 20000.0)
-      lt = p->lane == TSQ_LANE_AUTO && cta16_supported(out_mode, local, sc, p->gap_open, p->gap_extend) ? 4 : 3;
+    if (steps32 > 20000.0) lt = cta16 ? 4 : 3;
+  } else if (lt == 1 && cta16) {
+    const double steps16 = double((la + 511) / 512) * double(lb + 63);
+    if (steps16 > 20000.0) lt = 4;
   }
   ShapeChooser ch;
   ch.out_mode = out_mode;
