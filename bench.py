@@ -787,13 +787,13 @@ def traceback_uneven(O, A, W, cores, sample=2000):
         "checked": f"{sample} seeded pairs byte for byte: score, coordinates, identity, both gapped strings"}
 
 
-def long_pair_kernels(ps, per_sm=1):
+def long_pair_kernels(ps, per_sm=2):
     """Rooflines of the long-pair kernels: a device-resident batch of the
-    first long DNA pairs, per_sm of them per SM (the CTA fill's residency:
-    one 16-warp CTA per SM, so that every SM holds one pair) as far as their
-    traceback planes fit in 40 % of the free HBM (at most 120 GB): the CTA
-    traceback fill in int16x2 lanes, then one walker warp per pair, timed by
-    the batch's own events."""
+    first long DNA pairs, per_sm of them per SM (one 16-warp CTA is resident
+    per SM; the second pair per SM evens out the first pairs' uneven
+    lengths) as far as their traceback planes fit in 40 % of the free HBM
+    (at most 120 GB): the CTA traceback fill in int16x2 lanes, then one
+    walker warp per pair, timed by the batch's own events."""
     import torch
 
     from tweakseq_gb300 import aligner as A
@@ -832,7 +832,7 @@ def long_pair_kernels(ps, per_sm=1):
                          "traffic": traffic, "traffic_source": "ncu DRAM bytes of a 32-pair launch, scaled by cells",
                          "peak_source": "measured live: tsq_probe_dpx int16x2 rate x 2 cells / 4 DPX instructions "
                                         "per cell",
-                         "note": f"{n_pairs} pairs, one 16-warp CTA each, at most {per_sm} per SM"},
+                         "note": f"{n_pairs} pairs, one 16-warp CTA each, one CTA resident per SM"},
             "plane_writes": {"bound": "hbm", "achieved": plane_gbs, "peak": hbm, "unit": "GB/s",
                              "frac": plane_gbs / hbm, "bytes_per_cell": 0.5, "peak_source": hbm_src}},
         "walk_warp_kernel": {
