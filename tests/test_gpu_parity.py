@@ -480,7 +480,8 @@ def test_int16_cta_fill_rebased_values(output):
 
     big = prot(20000)
     prot_cases = [(b"W" * 16000, b"W" * 16000), (prot(16000), prot(15000)), (big, big[:8000] + big[12000:]),
-                  (prot(80000), prot(40)), (prot(513), prot(40000)), (prot(8193), prot(23000))]
+                  (prot(80000), prot(40)), (prot(200000), prot(1)), (prot(1), prot(30000)), (prot(512), prot(45000)),
+                  (prot(513), prot(40000)), (prot(8193), prot(23000))]
     d = W.DNA_LETTERS[rng.integers(0, 4, 30000)]
     dna_cases = [(d.tobytes(), W._mutate_dna(rng, d, 0.05, 0.01, 3.0)[:29000].tobytes()),
                  (W.DNA_LETTERS[rng.integers(0, 4, 20000)].tobytes(),
@@ -508,6 +509,16 @@ def test_int16_cta_fill_rebased_values(output):
             assert r.score == int(want["score"][len(ps) - 1])
             if output == "alignment":
                 assert (r.aln_a, r.aln_b) == (sa[-1], sb[-1])
+    # An invalid residue in a long pair: that pair reports it, the others
+    # of the launch are unaffected.
+    bad = bytearray(big)
+    bad[12345] = ord("*")
+    ps = W._pairset_from_lists([bytes(bad), big[:15000], big, big[:15000]], [(0, 1), (2, 3)])
+    got = A.align_batch(ps, output=output, check=False)
+    assert got.table["status"].tolist() == [N.E_INVALID_RESIDUE, 0]
+    want = O.batch(ps.seqs, ps.a_off[1:], ps.a_len[1:], ps.b_off[1:], ps.b_len[1:], O.BLOSUM62, 11, 1, False,
+                   O.MODE_SCORE, 0, False)
+    assert int(got.table["score"][1]) == int(want["score"][0])
 
 
 def test_alignment_batch_in_waves(monkeypatch):

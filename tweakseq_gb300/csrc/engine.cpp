@@ -1357,6 +1357,44 @@ int batch_collect(tsq_batch *b, int64_t begin, int64_t count, tsq_result *out, c
     }
     return rc;
   }
+  if (b->out_mode == kOutTrace && count >= 512) {
+    // Each pair's rows take two allocations and two copies: parallel over
+    // the pairs.  The status is the first failure to take rows (TSQ_E_CUDA,
+    // TSQ_E_NOMEM) if any, else what the serial loop below returns.
+    const int slices = int(std::min<int64_t>({8, int64_t(WorkerPool::get().workers()) + 1, count / 256}));
+    const int64_t step = (count + slices - 1) / slices;
+    struct Part {
+      int fail = TSQ_OK;
+      int last = TSQ_OK;
+      bool residue = false;
+    };
+    std::vector<Part> parts(static_cast<size_t>(slices));
+    run_slices(slices, [&](int sl) {
+      Part pt;
+      for (int64_t q = int64_t(sl) * step, e = std::min(count, q + step); q < e; ++q) {
+        const int64_t k = begin + q;
+        tsq_result &o = dst ? out[dst[q]] : out[q];
+        const ResultDev &d = r[k];
+        const PairDev &pd = b->pairs_h[size_t(k)];
+        const int e2 = collect_one(d, d.status == TSQ_OK ? b->aln_h.as<char>() + b->aln_off_h[size_t(k)] : nullptr,
+                                   int64_t(pd.a_len) + pd.b_len, o);
+        if (e2 != TSQ_OK && pt.fail == TSQ_OK) pt.fail = e2;
+        if (d.status == TSQ_E_INVALID_RESIDUE)
+          pt.residue = true;
+        else if (d.status != TSQ_OK)
+          pt.last = d.status;
+      }
+      parts[size_t(sl)] = pt;
+    });
+    for (const Part &pt : parts)
+      if (pt.fail != TSQ_OK) return pt.fail;
+    int rc = TSQ_OK;
+    for (const Part &pt : parts) {
+      if (pt.residue && rc == TSQ_OK) rc = TSQ_E_INVALID_RESIDUE;
+      if (pt.last != TSQ_OK) rc = pt.last;
+    }
+    return rc;
+  }
   int rc = TSQ_OK;
   for (int64_t q = 0; q < count; ++q) {
     const int64_t k = begin + q;
