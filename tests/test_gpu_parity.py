@@ -241,6 +241,19 @@ def test_custom_matrix_asymmetric():
                                O.MODE_ALIGN, 0, True)
         assert_same(got, want, FIELDS, "custom")
         assert got.aln_a == sa and got.aln_b == sb
+    # Long pairs over all 25 valid letters: 25 score classes, whose profile
+    # takes the 8-warp variant of the int16x2 CTA fill.
+    letters = np.frombuffer(bytes(c for c in range(65, 91) if c != ord("Z")), dtype=np.uint8)
+    seqs = [letters[rng.integers(0, len(letters), L)].tobytes() for L in (9000, 8000, 12000, 700)]
+    ps = W._pairset_from_lists(seqs, [(0, 1), (2, 3)])
+    for output, omode in (("score", O.MODE_SCORE), ("alignment", O.MODE_ALIGN)):
+        got = A.align_batch(ps, custom=(mat, valid), gap_open=4, gap_extend=2, output=output)
+        want = O.batch(ps.seqs, ps.a_off, ps.a_len, ps.b_off, ps.b_len, (mat, valid), 4, 2, False, omode, 0,
+                       omode == O.MODE_ALIGN)
+        if omode == O.MODE_ALIGN:
+            want, sa, sb = want
+            assert got.aln_a == sa and got.aln_b == sb
+        assert_same(got, want, FIELDS if omode == O.MODE_ALIGN else ("score",), f"custom long {output}")
 
 
 def test_graph_replay_and_device_resident_batch():
