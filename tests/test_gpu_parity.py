@@ -476,23 +476,28 @@ def test_long_pairs_on_the_cta_fill_all_outputs(local):
     assert (r.score, r.aln_a, r.aln_b) == (int(want["score"][2]), sa[2], sb[2])
 
 
+@pytest.mark.parametrize("local", [False, True])
 @pytest.mark.parametrize("output", ["score", "alignment"])
-def test_int16_cta_fill_rebased_values(output):
-    """Long global pairs on the CTA fill in int16x2 lanes, whose values are
-    kept relative to a moving base: scores far past the int16 range upwards
+def test_int16_cta_fill_rebased_values(output, local):
+    """Long pairs on the CTA fill in int16x2 lanes, whose values are kept
+    relative to a moving base: scores far past the int16 range upwards
     (W:W, 176,000) and downwards, a 4,000-residue gap, a 40-column pair (no
     interior steps), 513 rows (a one-row second pass), 17 passes (the
-    wrap-around row), BLOSUM62 (23 classes, 16 warps) and DNA, against the
-    oracle; gap costs at the bound (open + ext + max score = 40) and past it
-    (the int32 CTA fill).  The plain form of a long pair takes the same
-    kernel."""
+    wrap-around row), BLOSUM62 (23 classes, 16 warps global, 8 local) and
+    DNA, against the oracle; gap costs at the bound (open + ext + max score
+    = 40) and past it (the int32 CTA fill).  Local mode: a 5,000-residue
+    identical block followed by 12,000 unrelated residues (the maximum far
+    behind the base when the fill ends).  The plain form of a long pair
+    takes the same kernel."""
     rng = np.random.default_rng(61)
 
     def prot(n):
         return W.random_protein(rng, n).tobytes()
 
     big = prot(20000)
+    block = prot(5000)
     prot_cases = [(b"W" * 16000, b"W" * 16000), (prot(16000), prot(15000)), (big, big[:8000] + big[12000:]),
+                  (block + prot(12000), block + prot(12000)),
                   (prot(80000), prot(40)), (prot(200000), prot(1)), (prot(1), prot(30000)), (prot(512), prot(45000)),
                   (prot(513), prot(40000)), (prot(8193), prot(23000))]
     d = W.DNA_LETTERS[rng.integers(0, 4, 30000)]
@@ -500,7 +505,8 @@ def test_int16_cta_fill_rebased_values(output):
                  (W.DNA_LETTERS[rng.integers(0, 4, 20000)].tobytes(),
                   W.DNA_LETTERS[rng.integers(0, 4, 20000)].tobytes())]
     omode = O.MODE_ALIGN if output == "alignment" else O.MODE_SCORE
-    fields = FIELDS if output == "alignment" else ("score",)
+    fields = FIELDS if output == "alignment" else score_fields(local)
+    mode = "local" if local else "global"
     for cases, matrix, gaps in ((prot_cases, "blosum62", ((11, 1), (25, 4), (27, 4))),
                                 (dna_cases, "dna", ((5, 2),))):
         seqs, pairs = [], []
@@ -510,15 +516,16 @@ def test_int16_cta_fill_rebased_values(output):
         ps = W._pairset_from_lists(seqs, pairs)
         which = O.DNA if matrix == "dna" else O.BLOSUM62
         for go, ge in gaps:
-            want = O.batch(ps.seqs, ps.a_off, ps.a_len, ps.b_off, ps.b_len, which, go, ge, False, omode, 0,
+            want = O.batch(ps.seqs, ps.a_off, ps.a_len, ps.b_off, ps.b_len, which, go, ge, local, omode, 0,
                            output == "alignment")
             if output == "alignment":
                 want, sa, sb = want
-            got = A.align_batch(ps, matrix=matrix, gap_open=go, gap_extend=ge, output=output)
-            assert_same(got, want, fields, f"{matrix} {go}/{ge}")
+            got = A.align_batch(ps, matrix=matrix, gap_open=go, gap_extend=ge, mode=mode, output=output)
+            assert_same(got, want, fields, f"{matrix} {go}/{ge} {mode}")
             if output == "alignment":
-                assert got.aln_a == sa and got.aln_b == sb, f"{matrix} {go}/{ge}"
-            r = A.align_pair(*ps.pair(len(ps) - 1), matrix=matrix, gap_open=go, gap_extend=ge, output=output)
+                assert got.aln_a == sa and got.aln_b == sb, f"{matrix} {go}/{ge} {mode}"
+            r = A.align_pair(*ps.pair(len(ps) - 1), matrix=matrix, gap_open=go, gap_extend=ge, mode=mode,
+                             output=output)
             assert r.score == int(want["score"][len(ps) - 1])
             if output == "alignment":
                 assert (r.aln_a, r.aln_b) == (sa[-1], sb[-1])
@@ -527,9 +534,9 @@ def test_int16_cta_fill_rebased_values(output):
     bad = bytearray(big)
     bad[12345] = ord("*")
     ps = W._pairset_from_lists([bytes(bad), big[:15000], big, big[:15000]], [(0, 1), (2, 3)])
-    got = A.align_batch(ps, output=output, check=False)
+    got = A.align_batch(ps, mode=mode, output=output, check=False)
     assert got.table["status"].tolist() == [N.E_INVALID_RESIDUE, 0]
-    want = O.batch(ps.seqs, ps.a_off[1:], ps.a_len[1:], ps.b_off[1:], ps.b_len[1:], O.BLOSUM62, 11, 1, False,
+    want = O.batch(ps.seqs, ps.a_off[1:], ps.a_len[1:], ps.b_off[1:], ps.b_len[1:], O.BLOSUM62, 11, 1, local,
                    O.MODE_SCORE, 0, False)
     assert int(got.table["score"][1]) == int(want["score"][0])
 

@@ -712,8 +712,8 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
   // or 8 warps of a CTA):
   // those whose sweep on one 32-lane group -- ceil(m/256) bands of n+31
   // steps -- would outlast the batch's balanced per-lane work (or, alone,
-  // 20,000 steps).  Under the automatic lane type, global score and
-  // traceback pairs take the CTA fill in int16x2 lanes with rebased values
+  // 20,000 steps).  Under the automatic lane type, score and traceback
+  // pairs take the CTA fill in int16x2 lanes with rebased values
   // (fill_cta16.cuh) when open + ext + max_score <= 40: the long int32
   // pairs, and the int16x2 pairs whose sweep on one 32-lane group --
   // ceil(m/512) passes of n+63 steps -- exceeds the same budget.
@@ -884,7 +884,7 @@ int plan_impl(tsq_batch *b, const tsq_batch *owner, const uint8_t *seqs, int64_t
       L.cta = true;
       L.task_begin = int32_t(s);
       L.n_wtasks = int32_t(e - s);
-      const int max_blocks = lt == 4 ? cta16_blocks(b->out_mode, sc.nclasses) : cta_blocks(b->out_mode, b->local);
+      const int max_blocks = lt == 4 ? cta16_blocks(b->out_mode, b->local, sc.nclasses) : cta_blocks(b->out_mode, b->local);
       if (max_blocks <= 0) return TSQ_E_CUDA;
       L.blocks = int32_t(std::max<int64_t>(1, std::min<int64_t>(max_blocks, e - s)));
       L.bnd_cols = ((cols + 31) / 32 + 1) * 32;
@@ -1134,7 +1134,7 @@ int enqueue_run(tsq_batch *b) {
         a.ccodes = ccodes_dev(b);
         a.cmatrix = b->cmatrix.as<int8_t>();
         a.nclasses = b->scheme.nclasses;
-        TSQ_TRY(launch_cta16(b->out_mode, a, L.blocks, b->side));
+        TSQ_TRY(launch_cta16(b->out_mode, b->local, a, L.blocks, b->side));
       } else {
         TSQ_TRY(launch_cta(b->out_mode, b->local, a, L.blocks, b->side));
       }

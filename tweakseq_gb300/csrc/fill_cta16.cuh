@@ -1,5 +1,5 @@
 // fill_cta16.cuh -- one long pair per CTA in int16x2 lanes with rebased
-// values (global alignment; score or traceback output).
+// values (global or local alignment; score or traceback output).
 //
 // Rows go in passes of 512.  Lane t of a warp holds rows 512p + 8t .. +7
 // (band A, low halves) and 512p + 256 + 8t .. +7 (band B, high halves),
@@ -24,6 +24,14 @@
 // +-26,000 of the base.  Ring entries are converted to the warp's base as
 // lane 0 reads them, and the bottom row back to absolute values as lane 31
 // writes it.
+//
+// Local mode.  H's floor, 0, is -base on a warp's scale (held at the int16
+// floor when the base is higher: the live values are then all positive).
+// A local maximum may lie far from the current base, so the per-row maxima
+// of the last 32 steps are folded into one absolute (score, row, column)
+// key per lane at every move of the base, and then start again; the keys of
+// all lanes and warps give the pair's maximum, first in row-major order on
+// ties, as the other fills do.
 //
 // Every wait is bounded, as in the int32 CTA fill: a wait that runs out
 // marks the pair TSQ_E_TIMEOUT and makes every other wait of the CTA give
@@ -63,7 +71,7 @@ __device__ __forceinline__ void stage_codes16(int k, int t, int n, const uint8_t
   if ((a & (kCodeRing16 - 1)) == 0) cp_async16(code_ring + kCodeRing16, codes + a);
 }
 
-template <int OUT, int W>
+template <int OUT, int W, bool LOCAL>
 __global__ void __launch_bounds__(W * 32, 1) fill_cta16_kernel(const FillArgs A) {
   static_assert(OUT == kOutScore || OUT == kOutTrace, "score and traceback output");
   constexpr int G = 32, R = 8, P = G * R, P2 = 2 * P;
@@ -82,6 +90,7 @@ __global__ void __launch_bounds__(W * 32, 1) fill_cta16_kernel(const FillArgs A)
   volatile int *cons = prod + W;                              // [W]
   volatile int *fail = cons + W;
   int *s_misc = const_cast<int *>(fail) + 1;  // task index
+  uint64_t *s_keys = reinterpret_cast<uint64_t *>(p + cta_keys_offset(W));  // [W] local maxima
 
   for (int k = threadIdx.x; k < kMatBytes16; k += blockDim.x) {
     const int x = k / kMatRow16, c = k % kMatRow16;
@@ -134,7 +143,7 @@ __global__ void __launch_bounds__(W * 32, 1) fill_cta16_kernel(const FillArgs A)
     if constexpr (OUT == kOutTrace) planes = reinterpret_cast<uint32_t *>(A.planes + A.plane_off[pid]);
     (void)planes, (void)nbands;
     if (!trivial)
-      for (int j = threadIdx.x; j < n; j += blockDim.x) grow[j] = make_int2(edge_h(j + 1, go, ge, false), kNegInf);
+      for (int j = threadIdx.x; j < n; j += blockDim.x) grow[j] = make_int2(edge_h(j + 1, go, ge, LOCAL), kNegInf);
     if (threadIdx.x < W) {
       prod[threadIdx.x] = 0;
       cons[threadIdx.x] = 0;
@@ -143,6 +152,7 @@ __global__ void __launch_bounds__(W * 32, 1) fill_cta16_kernel(const FillArgs A)
     __syncthreads();
 
     int32_t last_h = 0;
+    uint64_t lkey = 0;  // local: this lane's maximum so far, as (score, -row, -column)
     const int2 *ring_in = w > 0 ? rings + (w - 1) * kCtaRing : nullptr;  // written by warp w-1
     int2 *ring_out = w < W - 1 ? rings + w * kCtaRing : nullptr;         // read by warp w+1
 
@@ -187,15 +197,50 @@ __global__ void __launch_bounds__(W * 32, 1) fill_cta16_kernel(const FillArgs A)
 
       // The warp's values are relative to bw (absolute); it starts at the
       // pass's top-left cell H(512p, 0).
-      int32_t bw = edge_h(pass * P2, go, ge, false);
+      int32_t bw = edge_h(pass * P2, go, ge, LOCAL);
+      // Local: H's floor 0, and 0 - open - ext, on the warp's scale.
+      uint32_t zero2 = 0u, zero_oe2 = 0u;
+      auto set_zero = [&]() {
+        const uint32_t z = uint32_t(max(-bw, kNeg16) + kBias16), zo = uint32_t(max(-bw - oe, kNeg16) + kBias16);
+        zero2 = (z << 16) | z;
+        zero_oe2 = (zo << 16) | zo;
+      };
+      if constexpr (LOCAL) set_zero();
       uint32_t H[R], E[R], T[R];
+      uint32_t best[R], bstep[R];  // local: per row, the best H of this window and its step (offset in the window)
+      (void)best, (void)bstep;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        H[r] = pack2b(edge_h(rowA + r + 1, go, ge, false) - bw, edge_h(rowB + r + 1, go, ge, false) - bw);
+        H[r] = pack2b(edge_h(rowA + r + 1, go, ge, LOCAL) - bw, edge_h(rowB + r + 1, go, ge, LOCAL) - bw);
         T[r] = __viaddmax_u16x2(H[r], noe2, kNeg2);
         E[r] = kNeg2;
+        if constexpr (LOCAL) {
+          best[r] = zero2;
+          bstep[r] = 0u;
+        }
       }
-      uint32_t hdiag = pack2b(edge_h(rowA, go, ge, false) - bw, edge_h(rowB, go, ge, false) - bw);
+      uint32_t hdiag = pack2b(edge_h(rowA, go, ge, LOCAL) - bw, edge_h(rowB, go, ge, LOCAL) - bw);
+      int sw = 0;  // local: first step of the current window
+      // Local: folds the window's row maxima (above 0, in rows of a) into
+      // the lane's key; columns from the step, 1-based.
+      auto fold = [&]() {
+        if constexpr (LOCAL) {
+#pragma unroll
+          for (int half = 0; half < 2; ++half) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+              const int row = (half ? rowB : rowA) + r;  // 0-based
+              const int32_t v = (half ? hi16b(best[r]) : lo16b(best[r])) + bw;
+              const int32_t col = sw + int32_t(half ? bstep[r] >> 16 : bstep[r] & 0xFFFFu) - t - (half ? G : 0) + 1;
+              if (row < m && v > 0) {
+                const uint64_t key = (uint64_t(uint32_t(v)) << 40) | (uint64_t(0xFFFFFu - uint32_t(row + 1)) << 20) |
+                                     uint64_t(0xFFFFFu - uint32_t(col));
+                lkey = key > lkey ? key : lkey;
+              }
+            }
+          }
+        }
+      };
       uint32_t outH = kBias2, outF = kNeg2;
       const int nS = n + G - 1;
       const int64_t wordA = ((int64_t)(2 * pass) * nS) * G + t;
@@ -286,6 +331,7 @@ __global__ void __launch_bounds__(W * 32, 1) fill_cta16_kernel(const FillArgs A)
           // subtraction that never borrows, every half being at least
           // floor + delta after the max; for delta <= 0 an addition that
           // never carries, the live values being far below the top.)
+          fold();
           const int32_t delta = __shfl_sync(0xffffffffu, lo16b(H[0]), 0);
           const uint32_t nd2 = uint32_t(-delta) * 0x10001u;
           const uint32_t lift = uint32_t(kNeg16 + kBias16 + max(delta, 0));
@@ -302,6 +348,15 @@ __global__ void __launch_bounds__(W * 32, 1) fill_cta16_kernel(const FillArgs A)
           outF = shift(outF);
           tv[cur] = shift(tv[cur]);
           bw += delta;
+          if constexpr (LOCAL) {
+            set_zero();
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+              best[r] = zero2;
+              bstep[r] = 0u;
+            }
+            sw = s;
+          }
         }
         const uint32_t rH = __shfl_sync(0xffffffffu, outH, src_lane);
         const uint32_t rF = __shfl_sync(0xffffffffu, outF, src_lane);
@@ -326,7 +381,10 @@ __global__ void __launch_bounds__(W * 32, 1) fill_cta16_kernel(const FillArgs A)
           uint32_t fv = __viaddmax_u16x2(upF, nge2, xo0);
           uint32_t xo = 0u;
           uint32_t acc1 = 0xCCCCCCCCu, acc2 = 0xCCCCCCCCu;
-          (void)acc1, (void)acc2;
+          uint32_t nz1 = 0u, nz2w = 0u;  // local: rows whose H is above 0
+          (void)acc1, (void)acc2, (void)nz1, (void)nz2w;
+          const uint32_t step2 = uint32_t(s - sw) * 0x10001u;  // local: the step in both halves
+          (void)step2;
           auto sweep = [&](auto masked_tag, uint32_t keep) {
             constexpr bool MASKED = decltype(masked_tag)::value;
 #pragma unroll
@@ -343,9 +401,9 @@ __global__ void __launch_bounds__(W * 32, 1) fill_cta16_kernel(const FillArgs A)
               }
               const uint32_t fo = r == 0 ? xo0 : xo;  // F's open candidate
               const uint32_t f = r == 0 ? fv : __viaddmax_u16x2(fv, nge2, xo);
-              uint32_t h = __vimax3_u16x2(x, f, f);
+              uint32_t h = LOCAL ? __vimax3_u16x2(x, f, zero2) : __vimax3_u16x2(x, f, f);
               uint32_t tn = sub2_imad(h, one, neg_oe2);
-              xo = sub2_imad(x, one, neg_oe2);
+              xo = LOCAL ? __viaddmax_u16x2(x, noe2, zero_oe2) : sub2_imad(x, one, neg_oe2);
               (void)fo;
               if constexpr (OUT == kOutTrace) {
                 // dir = [h > dd] + [h > x]; bits 2 and 3 clear when E / F
@@ -358,11 +416,29 @@ __global__ void __launch_bounds__(W * 32, 1) fill_cta16_kernel(const FillArgs A)
                   acc1 = imad(c, wgt, acc1);
                 else
                   acc2 = imad(c, wgt, acc2);
+                if constexpr (LOCAL) {
+                  const uint32_t z = nz2(h, zero2, minus_one, k1);
+                  if (r < 4)
+                    nz1 = imad(z, wgt, nz1);
+                  else
+                    nz2w = imad(z, wgt, nz2w);
+                }
               }
               if constexpr (MASKED) {
                 h = (h & ~keep) | (H[r] & keep);
                 tn = (tn & ~keep) | (T[r] & keep);
                 e = (e & ~keep) | (E[r] & keep);
+              }
+              if constexpr (LOCAL) {
+                // Halves where this cell beats the row's best of the window
+                // (strictly: the first column of a maximum is kept); a half
+                // outside its column range keeps an old value and records
+                // nothing.
+                const uint32_t nb = __vimax3_u16x2(best[r], h, h);
+                uint32_t cm = imad(nz2(nb, best[r], minus_one, k1), 0xFFFFu * one, 0u);
+                if constexpr (MASKED) cm &= ~keep;
+                best[r] = (nb & cm) | (best[r] & ~cm);
+                bstep[r] = (bstep[r] & ~cm) | (step2 & cm);
               }
               d = H[r];
               H[r] = h;
@@ -392,6 +468,11 @@ __global__ void __launch_bounds__(W * 32, 1) fill_cta16_kernel(const FillArgs A)
               out_ring[(base + jB) % kCtaRing] = v;
           }
           if constexpr (OUT == kOutTrace) {
+            if constexpr (LOCAL) {
+              // A local stop (H = 0) has direction 3.
+              acc1 |= (0x11111111u - nz1) * 3u;
+              acc2 |= (0x11111111u - nz2w) * 3u;
+            }
             if (vA) planes[wordA + (int64_t)s * G] = prmt(acc1, acc2, 0x5410u);
             if (vB && hasB) planes[wordB + (int64_t)s * G] = prmt(acc1, acc2, 0x7632u);
           }
@@ -445,7 +526,8 @@ __global__ void __launch_bounds__(W * 32, 1) fill_cta16_kernel(const FillArgs A)
         __threadfence_block();
         cons[w] = base + n;
       }
-      if (pass == passes - 1) {
+      fold();
+      if (!LOCAL && pass == passes - 1) {
         const int wr = (m - 1) - pass * P2;  // row m within this pass
         const int half = wr >= P ? 1 : 0;
         const int lr = (wr - half * P) - t * R;
@@ -457,6 +539,25 @@ __global__ void __launch_bounds__(W * 32, 1) fill_cta16_kernel(const FillArgs A)
 
     // ---- result (every warp has finished its passes) --------------------
     __syncthreads();
+    if constexpr (LOCAL) {
+      const uint64_t wkey = group_max<32>(lkey);
+      if (lane == 0) s_keys[w] = wkey;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        uint64_t gkey = 0;
+        for (int q = 0; q < W; ++q) gkey = s_keys[q] > gkey ? s_keys[q] : gkey;
+        ResultDev &o = A.res[pid];
+        o.status = gbad ? TSQ_E_INVALID_RESIDUE : (*fail ? TSQ_E_TIMEOUT : TSQ_OK);
+        const int32_t sc = int32_t(gkey >> 40);
+        o.score = sc;
+        o.a_end = sc > 0 ? int32_t(0xFFFFFu - uint32_t((gkey >> 20) & 0xFFFFFu)) : 0;
+        o.b_end = sc > 0 ? int32_t(0xFFFFFu - uint32_t(gkey & 0xFFFFFu)) : 0;
+        o.a_begin = o.b_begin = sc > 0 ? -1 : 0;
+        o.n_ident = o.n_cols = -1;
+      }
+      __syncthreads();
+      continue;
+    }
     const int last_w = passes > 0 ? (passes - 1) % W : 0;
     const int wr = m > 0 ? (m - 1) % P2 : 0;
     const int owner_t = (wr % P) / R;

@@ -131,7 +131,7 @@ int pair_align(PairPath *pp, const uint8_t *a, int32_t la, const uint8_t *b, int
 
   // Resident blocks of the kernel: the query also opts it into its shared
   // memory (answered from a cache after the first call).
-  const int blocks_avail = lt == 4   ? cta16_blocks(out_mode, sc.nclasses)
+  const int blocks_avail = lt == 4   ? cta16_blocks(out_mode, local, sc.nclasses)
                            : lt == 3 ? cta_blocks(out_mode, local)
                                      : fill_blocks(kFillRows, i16, out_mode, local, i16 ? sc.nclasses : kLetters);
   if (blocks_avail <= 0) return TSQ_E_CUDA;
@@ -208,7 +208,7 @@ int pair_align(PairPath *pp, const uint8_t *a, int32_t la, const uint8_t *b, int
     fa.nclasses = sc.nclasses;
   }
   if (lt == 4) {
-    PAIR_TRY(launch_cta16(out_mode, fa, 1, st));
+    PAIR_TRY(launch_cta16(out_mode, local, fa, 1, st));
   } else if (lt == 3) {
     PAIR_TRY(launch_cta(out_mode, local, fa, 1, st));
   } else {

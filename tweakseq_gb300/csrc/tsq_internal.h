@@ -145,12 +145,12 @@ bool shape_supported(const Shape &sh, int out_mode, bool local);
 int cta_blocks(int out_mode, bool local);
 size_t cta_bnd_entry_bytes(int out_mode);
 cudaError_t launch_cta(int out_mode, bool local, const FillArgs &a, int blocks, cudaStream_t st);
-// The same in int16x2 lanes with rebased values (fill_cta16.cu): global
-// score and traceback output, open + ext + max_score <= 40.  FillArgs
-// also carries the class codes, class matrix and class count.
+// The same in int16x2 lanes with rebased values (fill_cta16.cu): score and
+// traceback output, global or local, open + ext + max_score <= 40.
+// FillArgs also carries the class codes, class matrix and class count.
 bool cta16_supported(int out_mode, bool local, const Scheme &sc, int32_t gap_open, int32_t gap_extend);
-int cta16_blocks(int out_mode, int nclasses);
-cudaError_t launch_cta16(int out_mode, const FillArgs &a, int blocks, cudaStream_t st);
+int cta16_blocks(int out_mode, bool local, int nclasses);
+cudaError_t launch_cta16(int out_mode, bool local, const FillArgs &a, int blocks, cudaStream_t st);
 cudaError_t launch_walk(const WalkArgs &a, cudaStream_t st);
 // Residues -> letter codes and, when clut_dev / ccodes are set, score
 // classes.
