@@ -64,7 +64,7 @@ def parse_args():
     ap.add_argument("--msa-only", action="store_true", help="run only the consensus and guide-tree legs")
     ap.add_argument("--profile-lane", choices=["auto", "i16", "i32"], default="auto",
                     help="lane type of the --profile-case batch")
-    ap.add_argument("--profile-case", choices=["long_dna", "identity", "consensus", "uniform", "traceback"],
+    ap.add_argument("--profile-case", choices=["long_dna", "identity", "consensus", "uniform", "traceback", "plain"],
                     default=None,
                     help="small profiling case of another kernel (for ncu)")
     return ap.parse_args()
@@ -945,7 +945,9 @@ def run_profile_case(args):
     traceback fill and the walker), consensus (100,000 x 2,000 alignment:
     the class-count kernel),
     uniform (20,000 protein pairs of 320 x 2,000: the int16x2 score fill with
-    interior steps only, for instruction counts per step).
+    interior steps only, for instruction counts per step),
+    plain (tsq_align_pair at the C ABI on the first 200 uneven pairs, score
+    then alignment: the one-pair path's kernels per call).
     Device-resident, no graph, warm-up then timed runs."""
     import torch
 
@@ -984,6 +986,27 @@ def run_profile_case(args):
             st = b.stats()
         print(json.dumps({"profile_case": case, "pairs": len(ps), "cells": ps.cells, "fill_ms": st["fill_ms"],
                           "device_ms": st["device_ms"], "fill_gcups": ps.cells / (st["fill_ms"] * 1e-3) / 1e9}))
+        return
+    if case == "plain":
+        ps = W.uneven_pairs().subset(np.arange(200))
+        L = N.lib()
+        base = ps.seqs.ctypes.data
+        res = N.Result()
+        out = {"profile_case": case, "pairs": len(ps), "cells": ps.cells}
+        for output in ("score", "alignment"):
+            params, keep = N.make_params(output=output)
+            times = []
+            for it in range(args.warmup + args.steps):
+                t0 = time.perf_counter()
+                for k in range(len(ps)):
+                    rc = L.tsq_align_pair(base + int(ps.a_off[k]), int(ps.a_len[k]), base + int(ps.b_off[k]),
+                                          int(ps.b_len[k]), ctypes.byref(params), ctypes.byref(res))
+                    assert rc == 0
+                    L.tsq_result_free(ctypes.byref(res))
+                times.append(time.perf_counter() - t0)
+            t = float(np.median(times[args.warmup:])) if args.steps > 0 else float(times[-1])
+            out[output] = {"ms_per_pair": t / len(ps) * 1e3, "gcups": ps.cells / t / 1e9}
+        print(json.dumps(out))
         return
     if case == "consensus":
         nseq, ncols = 100_000, 2000
