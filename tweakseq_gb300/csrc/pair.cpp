@@ -154,6 +154,8 @@ int pair_align(PairPath *pp, const uint8_t *a, int32_t la, const uint8_t *b, int
   const int64_t dev_bytes = off_planes + std::max<int64_t>(plane_total, 16);
 
   auto grow = [](size_t need, size_t cap) { return need <= cap ? need : need + need / 2; };
+  // (A pair whose traceback planes do not fit in device memory fails here
+  // with TSQ_E_NOMEM, as it does on the batch engine's one-pair plan.)
   PAIR_TRY(pp->dev.ensure(grow(size_t(dev_bytes), pp->dev.cap), st));
   PAIR_TRY(pp->up.ensure(grow(size_t(up_bytes), pp->up.cap)));
   PAIR_TRY(pp->down.ensure(grow(size_t(down_bytes), pp->down.cap)));
