@@ -294,7 +294,7 @@ def test_one_pair_path_every_kind(output):
 
     cases = [(b"", prot(30)), (prot(25), b""), (b"", b""), (prot(1), prot(1)), (prot(300), prot(500)),
              (prot(900), prot(40)), (b"W" * 2900, b"W" * 2900), (b"W" * 3100, b"W" * 3100),
-             (prot(3000), prot(2600)), (prot(64), prot(70))]
+             (prot(3000), prot(2600)), (prot(64), prot(70)), (prot(600), prot(500)), (prot(1100), prot(900))]
     seqs, pairs = [], []
     for a, b in cases:
         seqs += [a, b]
